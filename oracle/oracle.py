@@ -1,0 +1,138 @@
+"""ctypes front-end of the C oracle (kcv_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the product library never imports this module.  It is
+used by tests/ as the parity checker, by ``__graft_entry__.smoke()`` as the
+checker of the smoke run, and by ``bench.py`` for the CPU baseline
+("port", since the reference itself is AArch64-only C++ that neither this
+container nor the GPU machine can build from its sources).
+
+Images are 2-D numpy arrays whose first axis is the row; row strides are taken
+from ``array.strides[0]`` so padded layouts (stride > width*channels*elem) are
+passed through exactly like the C API's ``src_stride`` / ``dst_stride``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libkcv_oracle.so")
+
+OK, NOT_IMPLEMENTED, NULL_POINTER, RANGE, ALLOCATION, ALIGNMENT = 0, 1, 2, 3, 4, 5
+CONSTANT, REPLICATE, REFLECT, WRAP, REVERSE, TRANSPARENT, NONE = range(7)
+FIXED_BORDERS = (REPLICATE, REFLECT, WRAP, REVERSE)
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with the recipe in oracle/Makefile."""
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+        os.path.getmtime(os.path.join(HERE, f)) for f in ("kcv_oracle.c", "kcv_oracle.h", "Makefile")
+    ):
+        subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        sz, vp, f, i = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_int
+        _lib.ko_gaussian_half_kernel.argtypes = [vp, sz, f]
+        _lib.ko_border_map.argtypes = [ctypes.c_long, ctypes.c_long, i]
+        _lib.ko_border_map.restype = ctypes.c_long
+        _lib.ko_border_table.argtypes = [i, ctypes.c_long, i, vp]
+        _lib.ko_gaussian_blur_u8.argtypes = [vp, sz, vp, sz, sz, sz, sz, sz, sz, f, f, i, i, i, i]
+        for name in ("ko_separable_filter_2d_u8", "ko_separable_filter_2d_u16"):
+            getattr(_lib, name).argtypes = [vp, sz, vp, sz, sz, sz, sz, vp, sz, vp, sz, i, i, i, i]
+        _lib.ko_separable_filter_2d_s16.argtypes = [vp, sz, vp, sz, sz, sz, sz, vp, sz, vp, sz, i, i, i]
+        _lib.ko_blur_and_downsample_u8.argtypes = [vp, sz, sz, sz, vp, sz, sz, i, i, i, i]
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _stride(a):
+    return 0 if a is None else int(a.strides[0])
+
+
+def half_kernel(ksize: int, sigma: float):
+    """Returns the half kernel (list of ksize//2+1 ints) or None for 'copy'."""
+    half = np.zeros(128, np.uint8)
+    ok = lib().ko_gaussian_half_kernel(half.ctypes.data, ksize // 2 + 1, float(sigma))
+    return [int(v) for v in half[: ksize // 2 + 1]] if ok else None
+
+
+def border_map(i: int, n: int, border: int) -> int:
+    return lib().ko_border_map(i, n, border)
+
+
+def border_table(ksize: int, n: int, border: int) -> np.ndarray:
+    out = np.zeros((n, ksize), np.int64)
+    lib().ko_border_table(ksize, n, border, out.ctypes.data)
+    return out
+
+
+def _out_like(src, width, height, channels, dtype, out_w=None, out_h=None):
+    ow = width if out_w is None else out_w
+    oh = height if out_h is None else out_h
+    return np.zeros((max(oh, 1), max(ow * channels, 1)), dtype)
+
+
+def gaussian_blur_u8(src, width, height, channels, ksize, sigma, border, *, ext=False,
+                     border_value=0, nthreads=1, dst=None, ksize_y=None, sigma_y=None):
+    if dst is None and src is not None:
+        dst = _out_like(src, width, height, channels, np.uint8)
+    err = lib().ko_gaussian_blur_u8(
+        _ptr(src), _stride(src), _ptr(dst), _stride(dst), width, height, channels, ksize,
+        ksize if ksize_y is None else ksize_y, float(sigma),
+        float(sigma if sigma_y is None else sigma_y), border, int(ext), int(border_value), nthreads)
+    return err, dst
+
+
+def separable_filter_2d(src, width, height, channels, kernel_x, kernel_y, border, *, ext=False,
+                        border_value=0, nthreads=1, dst=None, kw=None, kh=None):
+    dtype = src.dtype if src is not None else np.dtype(kernel_x.dtype)
+    if dst is None and src is not None:
+        dst = _out_like(src, width, height, channels, dtype)
+    kx = None if kernel_x is None else np.ascontiguousarray(kernel_x, dtype)
+    ky = None if kernel_y is None else np.ascontiguousarray(kernel_y, dtype)
+    kw = (len(kx) if kx is not None else 5) if kw is None else kw
+    kh = (len(ky) if ky is not None else 5) if kh is None else kh
+    if dtype == np.uint8:
+        err = lib().ko_separable_filter_2d_u8(_ptr(src), _stride(src), _ptr(dst), _stride(dst), width, height,
+                                              channels, _ptr(kx), kw, _ptr(ky), kh, border, int(ext),
+                                              int(border_value), nthreads)
+    elif dtype == np.uint16:
+        err = lib().ko_separable_filter_2d_u16(_ptr(src), _stride(src), _ptr(dst), _stride(dst), width, height,
+                                               channels, _ptr(kx), kw, _ptr(ky), kh, border, int(ext),
+                                               int(border_value), nthreads)
+    elif dtype == np.int16:
+        err = lib().ko_separable_filter_2d_s16(_ptr(src), _stride(src), _ptr(dst), _stride(dst), width, height,
+                                               channels, _ptr(kx), kw, _ptr(ky), kh, border, int(border_value),
+                                               nthreads)
+    else:
+        raise TypeError(dtype)
+    return err, dst
+
+
+def blur_and_downsample_u8(src, width, height, channels, border, *, ext=False, border_value=0,
+                           nthreads=1, dst=None):
+    if dst is None and src is not None:
+        dst = _out_like(src, width, height, channels, np.uint8, (width + 1) // 2, (height + 1) // 2)
+    err = lib().ko_blur_and_downsample_u8(_ptr(src), _stride(src), width, height, _ptr(dst), _stride(dst),
+                                          channels, border, int(ext), int(border_value), nthreads)
+    return err, dst
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv)
+    print(LIB_PATH)
