@@ -1,0 +1,305 @@
+/*
+ * kleidicv_gpu.h -- GB300 (sm_103a) drop-in for KleidiCV's separable-filter
+ * hot path, exposed as a plain C ABI.
+ *
+ * Every drop-in entry point keeps the parameter list, the meaning of every
+ * argument, the kleidicv_error_t values and the order in which errors are
+ * detected of the KleidiCV function it replaces, and adds one trailing
+ * `kleidicv_gpu_context_t *ctx` argument (the analogue of the trailing
+ * `kleidicv_thread_multithreading mt` argument of KleidiCV's threaded API).
+ *
+ *  - src / dst are DEVICE pointers (cudaMalloc, a pool, or device-mapped
+ *    memory); strides are in bytes.
+ *  - Validation errors are returned synchronously, before any CUDA call.
+ *  - Work is enqueued asynchronously on the context's stream; KLEIDICV_OK
+ *    means "enqueued".  kleidicv_gpu_context_synchronize() waits and reports
+ *    device-side failures.
+ *  - There is no CPU fallback: a context can only be created on a CUDA device
+ *    that runs sm_103a code, and entry points fail with
+ *    KLEIDICV_GPU_ERROR_CUDA if the device work cannot be launched.
+ *
+ * Reference functions replaced (KleidiCV project paths):
+ *  kleidicv_gpu_gaussian_blur_u8         kleidicv/include/kleidicv/kleidicv.h:2159-2163
+ *                                        (kleidicv/src/filters/gaussian_blur_api.cpp:59-67)
+ *  kleidicv_gpu_separable_filter_2d_u8   kleidicv/include/kleidicv/kleidicv.h:2091-2095
+ *                                        (kleidicv/src/filters/separable_filter_2d_api.cpp:47-55)
+ *  kleidicv_gpu_separable_filter_2d_u16  kleidicv/include/kleidicv/kleidicv.h:2103-2107
+ *                                        (kleidicv/src/filters/separable_filter_2d_api.cpp:67-75)
+ *  kleidicv_gpu_blur_and_downsample_u8   kleidicv/include/kleidicv/kleidicv.h:2215-2218
+ *                                        (kleidicv/src/filters/blur_and_downsample_api.cpp:40-48)
+ * and, with the same argument lists, the threaded variants
+ *  kleidicv_thread_{gaussian_blur_u8,separable_filter_2d_u8,
+ *  separable_filter_2d_u16,blur_and_downsample_u8}
+ *                                        kleidicv_thread/include/kleidicv_thread/kleidicv_thread.h:457-485
+ * (the `mt` scheduler argument becomes the context).
+ */
+#ifndef KLEIDICV_GPU_H
+#define KLEIDICV_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error and border enums: identical values to kleidicv/include/kleidicv/ctypes.h:26-79.
+ * When the reference header is included first its definitions are used. */
+#ifndef KLEIDICV_CTYPES_H
+typedef enum {
+  KLEIDICV_OK = 0,
+  KLEIDICV_ERROR_NOT_IMPLEMENTED,
+  KLEIDICV_ERROR_NULL_POINTER,
+  KLEIDICV_ERROR_RANGE,
+  KLEIDICV_ERROR_ALLOCATION,
+  KLEIDICV_ERROR_ALIGNMENT,
+  KLEIDICV_ERROR_CONTEXT_MISMATCH,
+} kleidicv_error_t;
+
+typedef enum {
+  KLEIDICV_BORDER_TYPE_CONSTANT,
+  KLEIDICV_BORDER_TYPE_REPLICATE,
+  KLEIDICV_BORDER_TYPE_REFLECT,
+  KLEIDICV_BORDER_TYPE_WRAP,
+  KLEIDICV_BORDER_TYPE_REVERSE,
+  KLEIDICV_BORDER_TYPE_TRANSPARENT,
+  KLEIDICV_BORDER_TYPE_NONE,
+} kleidicv_border_type_t;
+#endif
+
+/* GPU-specific failures, returned as kleidicv_error_t values >= 0x100 so
+ * that 0..6 keep the reference's meaning. */
+#define KLEIDICV_GPU_ERROR_CUDA ((kleidicv_error_t)0x100)      /* a CUDA call failed */
+#define KLEIDICV_GPU_ERROR_NO_DEVICE ((kleidicv_error_t)0x101) /* no usable sm_103 device */
+#define KLEIDICV_GPU_ERROR_TIMEOUT ((kleidicv_error_t)0x102)   /* a device wait hit its limit */
+#define KLEIDICV_GPU_ERROR_BUSY ((kleidicv_error_t)0x103)      /* serving queue full */
+
+/* KLEIDICV_MAX_IMAGE_PIXELS and KLEIDICV_MAXIMUM_CHANNEL_COUNT, kleidicv.h:103,110 */
+#define KLEIDICV_GPU_MAX_IMAGE_PIXELS ((1ULL << 48) - 1)
+#define KLEIDICV_GPU_MAXIMUM_CHANNEL_COUNT 4
+
+/* ------------------------------------------------------------------------ */
+/* Context: device, stream, device memory pool, error flag.                 */
+
+typedef struct kleidicv_gpu_context kleidicv_gpu_context_t;
+
+/* Creates a context on `device` that enqueues work on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream).  pool_limit_bytes caps the
+ * context's device pool (0 = 40 GiB). */
+kleidicv_error_t kleidicv_gpu_context_create(kleidicv_gpu_context_t **ctx,
+                                             int device, void *stream,
+                                             size_t pool_limit_bytes);
+kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_context_set_stream(kleidicv_gpu_context_t *ctx,
+                                                 void *stream);
+void *kleidicv_gpu_context_get_stream(const kleidicv_gpu_context_t *ctx);
+/* Waits for all work on the context's stream; reports CUDA errors and
+ * device-side timeouts recorded since the last call. */
+kleidicv_error_t kleidicv_gpu_context_synchronize(kleidicv_gpu_context_t *ctx);
+/* Fault injection for tests: the next `count` pool allocations fail. */
+void kleidicv_gpu_context_fail_next_allocations(kleidicv_gpu_context_t *ctx,
+                                                int count);
+/* Number of this library's kernels launched through the context so far. */
+uint64_t kleidicv_gpu_context_launch_count(const kleidicv_gpu_context_t *ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Drop-in entry points.                                                    */
+
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, size_t kernel_width,
+    size_t kernel_height, float sigma_x, float sigma_y,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint8_t *kernel_x,
+    size_t kernel_width, const uint8_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u16(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint16_t *kernel_x,
+    size_t kernel_width, const uint16_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height,
+    uint8_t *dst, size_t dst_stride, size_t channels,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Extensions (no reference counterpart; semantics defined by this library,
+ * "parity unpinned"):
+ *  - KLEIDICV_BORDER_TYPE_CONSTANT with an explicit border_value: the image
+ *    is treated as padded with border_value on every side (the definition
+ *    the reference's own test framework uses, test/framework/border.cpp:369-415);
+ *  - the s16 separable filter, whose declaration exists in the reference
+ *    (kleidicv/include/kleidicv/filters/separable_filter_2d.h:34-43) without
+ *    a definition: 32-bit vertical accumulation with saturating adds in tap
+ *    order, 64-bit horizontal accumulation, saturation to s16.
+ * For the four fixed border types the _ex functions return exactly what the
+ * drop-in functions return.  Kernel taps (kernel_x / kernel_y) are HOST
+ * pointers in every separable entry point, as in the reference. */
+
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8_ex(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, size_t kernel_width,
+    size_t kernel_height, float sigma_x, float sigma_y,
+    kleidicv_border_type_t border_type, uint8_t border_value,
+    kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u8_ex(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint8_t *kernel_x,
+    size_t kernel_width, const uint8_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, uint8_t border_value,
+    kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u16_ex(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint16_t *kernel_x,
+    size_t kernel_width, const uint16_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, uint16_t border_value,
+    kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_s16_ex(
+    const int16_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const int16_t *kernel_x,
+    size_t kernel_width, const int16_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, int16_t border_value,
+    kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8_ex(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height,
+    uint8_t *dst, size_t dst_stride, size_t channels,
+    kleidicv_border_type_t border_type, uint8_t border_value,
+    kleidicv_gpu_context_t *ctx);
+
+/* Image pyramid: `levels` successive blur_and_downsample_u8 steps.  Level l
+ * (1-based) has size ((w_{l-1}+1)/2, (h_{l-1}+1)/2) and is written to
+ * dst[l-1] with stride dst_strides[l-1].  The caller of the reference builds
+ * the same pyramid by calling kleidicv_blur_and_downsample_u8 once per level
+ * (kleidicv/include/kleidicv/analysis/build_optical_flow_pyr_lk_pyramid.h:359-380).
+ * Validation is per level, in level order, with the drop-in's rules. */
+kleidicv_error_t kleidicv_gpu_build_pyramid_u8(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height,
+    size_t channels, size_t levels, uint8_t *const *dst,
+    const size_t *dst_strides, kleidicv_border_type_t border_type,
+    kleidicv_gpu_context_t *ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Batched execution: many independent filter requests of uneven sizes run
+ * through one persistent kernel that walks a device-side tile work-list.  A
+ * plan is built once (validation, tile list, tensor maps, tile shapes from
+ * the autotune table) and can be launched repeatedly; plan launches may be
+ * captured into a CUDA graph. */
+
+typedef enum {
+  KLEIDICV_GPU_OP_GAUSSIAN_BLUR_U8 = 0,
+  KLEIDICV_GPU_OP_SEPARABLE_FILTER_2D_U8 = 1,
+  KLEIDICV_GPU_OP_SEPARABLE_FILTER_2D_U16 = 2,
+  KLEIDICV_GPU_OP_SEPARABLE_FILTER_2D_S16 = 3,
+  KLEIDICV_GPU_OP_BLUR_AND_DOWNSAMPLE_U8 = 4,
+} kleidicv_gpu_op_t;
+
+typedef struct {
+  kleidicv_gpu_op_t op;
+  const void *src; /* device */
+  size_t src_stride;
+  void *dst; /* device */
+  size_t dst_stride;
+  size_t width, height, channels; /* source size, as in the drop-in calls */
+  size_t kernel_width, kernel_height;
+  float sigma_x, sigma_y;     /* gaussian */
+  int32_t kernel_x[5];        /* separable taps (value range of the op's type) */
+  int32_t kernel_y[5];
+  kleidicv_border_type_t border_type;
+  int32_t border_value;       /* CONSTANT border only (extension) */
+  int32_t allow_extensions;   /* 0: drop-in validation; 1: _ex validation */
+} kleidicv_gpu_request_t;
+
+typedef struct kleidicv_gpu_batch_plan kleidicv_gpu_batch_plan_t;
+
+/* Validates every request (statuses[i] receives each request's
+ * kleidicv_error_t, exactly what the corresponding single call would
+ * return) and builds a plan for the valid ones.  Returns KLEIDICV_OK if the
+ * plan was built (even if some requests were rejected). */
+kleidicv_error_t kleidicv_gpu_batch_plan_create(
+    const kleidicv_gpu_request_t *requests, size_t count,
+    kleidicv_error_t *statuses, kleidicv_gpu_batch_plan_t **plan,
+    kleidicv_gpu_context_t *ctx);
+/* Enqueues the plan: one persistent-kernel launch (plus its work-counter
+ * reset), on the context's stream.  use_graph != 0 replays a CUDA graph
+ * captured on first use. */
+kleidicv_error_t kleidicv_gpu_batch_plan_launch(kleidicv_gpu_batch_plan_t *plan,
+                                                int use_graph,
+                                                kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_batch_plan_destroy(kleidicv_gpu_batch_plan_t *plan);
+/* Number of tiles in the plan's work-list. */
+size_t kleidicv_gpu_batch_plan_tile_count(const kleidicv_gpu_batch_plan_t *plan);
+
+/* One-shot convenience: plan + launch + destroy (destroy is deferred until
+ * the launch has completed). */
+kleidicv_error_t kleidicv_gpu_batch_submit(const kleidicv_gpu_request_t *requests,
+                                           size_t count,
+                                           kleidicv_error_t *statuses,
+                                           kleidicv_gpu_context_t *ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Serving loop: requests arrive asynchronously, images stay resident in a
+ * capped device pool, requests are admitted by free bytes and by free
+ * in-flight slots, and every scheduling round launches one persistent batch
+ * for everything admitted since the previous round while earlier batches are
+ * still running (continuous batching over several streams). */
+
+typedef struct kleidicv_gpu_server kleidicv_gpu_server_t;
+
+typedef struct {
+  size_t pool_limit_bytes;    /* device pool cap (0 = 40 GiB) */
+  int max_inflight_batches;   /* batches allowed on the GPU at once (0 = 4) */
+  int max_batch_requests;     /* requests per batch (0 = 256) */
+  int max_queue;              /* pending requests before BUSY (0 = 65536) */
+} kleidicv_gpu_server_config_t;
+
+typedef struct {
+  uint64_t id;
+  kleidicv_error_t status;
+  double arrival_s, admitted_s, completed_s; /* server clock, seconds */
+} kleidicv_gpu_completion_t;
+
+kleidicv_error_t kleidicv_gpu_server_create(const kleidicv_gpu_server_config_t *config,
+                                            int device, kleidicv_gpu_server_t **server);
+kleidicv_error_t kleidicv_gpu_server_destroy(kleidicv_gpu_server_t *server);
+/* Allocates `bytes` of device memory from the server's pool (for request
+ * images).  Returns NULL when the pool cap would be exceeded. */
+void *kleidicv_gpu_server_alloc(kleidicv_gpu_server_t *server, size_t bytes);
+void kleidicv_gpu_server_free(kleidicv_gpu_server_t *server, void *ptr);
+/* Queues a request; returns its id in *id.  The request's src/dst must stay
+ * valid until its completion is reported. */
+kleidicv_error_t kleidicv_gpu_server_submit(kleidicv_gpu_server_t *server,
+                                            const kleidicv_gpu_request_t *request,
+                                            uint64_t *id);
+/* Copies up to `capacity` completions (in completion order) into `out`;
+ * waits up to timeout_ms for at least one.  Returns the number copied. */
+size_t kleidicv_gpu_server_poll(kleidicv_gpu_server_t *server,
+                                kleidicv_gpu_completion_t *out, size_t capacity,
+                                int timeout_ms);
+/* Seconds on the server clock (the clock the completion times use). */
+double kleidicv_gpu_server_now(const kleidicv_gpu_server_t *server);
+/* Waits until every submitted request has completed. */
+kleidicv_error_t kleidicv_gpu_server_drain(kleidicv_gpu_server_t *server);
+
+/* ------------------------------------------------------------------------ */
+/* Introspection (used by tests): the Gaussian half kernel this library
+ * derives from (kernel_size, sigma), with the reference's generator
+ * (kleidicv/include/kleidicv/filters/sigma.h:27-79).  Returns 1 and fills
+ * kernel_size/2+1 weights, or 0 for the "copy" case. */
+int kleidicv_gpu_gaussian_half_kernel(size_t kernel_size, float sigma,
+                                      uint8_t *half_kernel);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KLEIDICV_GPU_H */

@@ -1,0 +1,271 @@
+"""GPU parity: every entry point, through the C ABI, against the CPU oracle.
+
+Bit-exact for all integer results (tolerance 0): kernel sizes, sigmas,
+channel counts, all border types, minimum sizes (k-1), multi-strip widths,
+padded and misaligned layouts, and the reference's own known-answer tests.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.gpu_harness import device_image, device_output, padded, pyr_sizes, read_output
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+BORDERS = [1, 2, 3, 4]  # REPLICATE, REFLECT, WRAP, REVERSE
+
+
+@pytest.fixture(scope="module")
+def ctx(kcv):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    c = kcv.Context.for_torch(0)
+    yield c
+    c.close()
+
+
+def run_gaussian(kcv, ctx, host, w, h, c, k, sigma, border, *, bv=None, offset=0, dst_pad=7,
+                 dst_offset=0):
+    _keep, src_ptr, src_stride = device_image(torch, host, offset)
+    obuf, dptr, dstride = device_output(torch, h, w * c, np.uint8, dst_pad, dst_offset)
+    err = kcv.gaussian_blur_u8(src_ptr, src_stride, dptr, dstride, w, h, c, k, k, sigma, sigma, border,
+                               ctx, border_value=bv)
+    assert err == kcv.OK, kcv.ERROR_NAMES.get(err, err)
+    assert ctx.synchronize() == kcv.OK
+    return read_output(obuf, h, w * c, np.uint8, dstride, dst_offset)
+
+
+def check_gaussian(kcv, oracle, ctx, rng, w, h, c, k, sigma, border, bv=None, offset=0, pad=5,
+                   high=255, low=0):
+    host = padded(rng, h, w * c, np.uint8, pad, low=low, high=high)
+    got, pad_ok = run_gaussian(kcv, ctx, host, w, h, c, k, sigma, border, bv=bv, offset=offset)
+    err, want = oracle.gaussian_blur_u8(host, w, h, c, k, sigma, border, ext=bv is not None,
+                                        border_value=bv or 0, nthreads=8)
+    assert err == oracle.OK
+    assert pad_ok, "write outside the destination rows"
+    if not np.array_equal(got, want):
+        bad = np.argwhere(got != want)
+        raise AssertionError(f"{len(bad)} mismatches (w={w} h={h} c={c} k={k} s={sigma} b={border}); "
+                             f"first {bad[:4].tolist()} got {got[tuple(bad[0])]} want {want[tuple(bad[0])]}")
+
+
+@pytest.mark.parametrize("k", [3, 5, 7, 9, 15, 21])
+@pytest.mark.parametrize("sigma", [0.0, 1.5])
+@pytest.mark.parametrize("c", [1, 2, 3, 4])
+def test_gaussian_fixed_sizes(kcv, oracle, ctx, k, sigma, c):
+    rng = np.random.default_rng(k * 31 + c + int(sigma * 10))
+    for border in BORDERS:
+        for (w, h) in [(k - 1, k - 1), (k + 4, k + 2), (37, max(23, k - 1)), (603, k + 1),
+                       (131, 300)]:
+            check_gaussian(kcv, oracle, ctx, rng, w, h, c, k, sigma, border)
+
+
+@pytest.mark.parametrize("k,sigma", [(7, 1.5), (5, 0.0), (15, 2.5), (21, 4.0), (3, 0.7)])
+def test_gaussian_constant_border_extension(kcv, oracle, ctx, k, sigma):
+    rng = np.random.default_rng(k)
+    for c in (1, 3, 4):
+        for bv in (0, 17, 255):
+            check_gaussian(kcv, oracle, ctx, rng, 45, k + 3, c, k, sigma, 0, bv=bv)
+
+
+def test_gaussian_copy_case(kcv, oracle, ctx):
+    assert kcv.half_kernel(3, 0.1) is None  # all weight in the centre tap
+    rng = np.random.default_rng(1)
+    for c in (1, 4):
+        check_gaussian(kcv, oracle, ctx, rng, 50, 9, c, 3, 0.1, 2)
+
+
+@pytest.mark.parametrize("k,sigma", [(11, 0.0), (13, 2.2), (17, 3.0), (31, 5.0), (63, 0.0), (255, 40.0)])
+def test_gaussian_arbitrary_sizes(kcv, oracle, ctx, k, sigma):
+    rng = np.random.default_rng(k)
+    r = k // 2
+    wmin = (r + 7) // 8 * 8 + r
+    for c in (1, 3, 4):
+        for (w, h) in [(wmin, k - 1), (wmin + 9, k + 3), (300, max(12, k - 1))]:
+            check_gaussian(kcv, oracle, ctx, rng, w, h, c, k, sigma, 1)
+
+
+@pytest.mark.parametrize("k,i", [(59, 3103), (123, 3810), (137, 3614), (165, 3464), (131, 1459)])
+def test_gaussian_arbitrary_weights_not_summing_to_256(kcv, oracle, ctx, k, i):
+    """Kernels whose rounded weights sum to 257 (or 255): the reference's
+    vector paths saturate and its border/scalar paths wrap; near-white images
+    exercise both."""
+    sigma = float(np.float32(i) / np.float32(100))
+    hk = kcv.half_kernel(k, sigma)
+    assert hk is not None and 2 * sum(hk[:-1]) + hk[-1] != 256
+    rng = np.random.default_rng(k)
+    r = k // 2
+    wmin = (r + 7) // 8 * 8 + r
+    for c in (1, 2, 4):
+        for (w, h) in [(wmin, k - 1), (wmin + 33, k + 5)]:
+            check_gaussian(kcv, oracle, ctx, rng, w, h, c, k, sigma, 1, low=250, high=255)
+    # narrow rows (width*channels < 16 is impossible here since width >= 13),
+    # so also an image with a mid region narrower than one vector:
+    check_gaussian(kcv, oracle, ctx, rng, wmin + 1, k - 1, 1, k, sigma, 1, low=250, high=255)
+
+
+@pytest.mark.parametrize("offset", [1, 3, 8])
+def test_gaussian_misaligned_and_padded(kcv, oracle, ctx, offset):
+    rng = np.random.default_rng(offset)
+    for (k, sigma, c) in [(5, 0.0, 1), (7, 1.5, 4), (3, 0.0, 3)]:
+        for border in BORDERS:
+            check_gaussian(kcv, oracle, ctx, rng, 301, 17, c, k, sigma, border, offset=offset, pad=3)
+
+
+# ---------------------------------------------------------------------------
+SEP_DT = {"u8": np.uint8, "u16": np.uint16, "s16": np.int16}
+
+
+def run_separable(kcv, ctx, dt, host, w, h, c, kx, ky, border, bv=None, offset=0):
+    dtype = SEP_DT[dt]
+    _keep, sp, ss = device_image(torch, host, offset)
+    obuf, dp, ds = device_output(torch, h, w * c, dtype, 3)
+    err = kcv.separable_filter_2d(dt, sp, ss, dp, ds, w, h, c, kx, 5, ky, 5, border, ctx, border_value=bv)
+    assert err == kcv.OK, kcv.ERROR_NAMES.get(err, err)
+    assert ctx.synchronize() == kcv.OK
+    return read_output(obuf, h, w * c, dtype, ds)
+
+
+@pytest.mark.parametrize("dt", ["u8", "u16", "s16"])
+@pytest.mark.parametrize("c", [1, 2, 3, 4])
+def test_separable(kcv, oracle, ctx, dt, c):
+    dtype = SEP_DT[dt]
+    info = np.iinfo(dtype)
+    rng = np.random.default_rng(c * 7 + len(dt))
+    borders = BORDERS + ([0] if dt == "s16" else [])
+    for border in borders:
+        for (w, h) in [(4, 4), (13, 6), (211, 9), (1100, 5)]:
+            for trange in ((0, 4), (info.min, info.max)) if dt != "s16" else ((-4, 4), (info.min, info.max)):
+                kx = rng.integers(trange[0], trange[1] + 1, 5)
+                ky = rng.integers(trange[0], trange[1] + 1, 5)
+                host = padded(rng, h, w * c, dtype, 2)
+                bv = 17 if border == 0 else None
+                got, pad_ok = run_separable(kcv, ctx, dt, host, w, h, c, kx, ky, border, bv)
+                err, want = oracle.separable_filter_2d(host, w, h, c, kx.astype(dtype), ky.astype(dtype),
+                                                       border, ext=bv is not None, border_value=bv or 0)
+                assert err == oracle.OK
+                assert pad_ok
+                assert np.array_equal(got, want), (dt, c, border, w, h, trange)
+
+
+@pytest.mark.parametrize("dt", ["u8", "u16"])
+def test_separable_constant_extension(kcv, oracle, ctx, dt):
+    dtype = SEP_DT[dt]
+    rng = np.random.default_rng(3)
+    for c in (1, 4):
+        kx, ky = rng.integers(0, 5, 5), rng.integers(0, 5, 5)
+        host = padded(rng, 9, 40 * c, dtype, 0)
+        got, _ = run_separable(kcv, ctx, dt, host, 40, 9, c, kx, ky, 0, 17)
+        err, want = oracle.separable_filter_2d(host, 40, 9, c, kx.astype(dtype), ky.astype(dtype), 0,
+                                               ext=True, border_value=17)
+        assert err == 0 and np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("c", [1, 2, 3, 4])
+def test_blur_and_downsample(kcv, oracle, ctx, c):
+    rng = np.random.default_rng(c)
+    for border in BORDERS + [0]:
+        for (w, h) in [(4, 4), (5, 5), (161, 7), (9, 12), (777, 33), (1031, 8)]:
+            host = padded(rng, h, w * c, np.uint8, 3)
+            ow, oh = (w + 1) // 2, (h + 1) // 2
+            _k, sp, ss = device_image(torch, host)
+            obuf, dp, ds = device_output(torch, oh, ow * c, np.uint8, 5)
+            bv = 17 if border == 0 else None
+            err = kcv.blur_and_downsample_u8(sp, ss, w, h, dp, ds, c, border, ctx, border_value=bv)
+            assert err == kcv.OK
+            assert ctx.synchronize() == kcv.OK
+            got, pad_ok = read_output(obuf, oh, ow * c, np.uint8, ds)
+            e2, want = oracle.blur_and_downsample_u8(host, w, h, c, border, ext=bv is not None,
+                                                     border_value=bv or 0)
+            assert e2 == 0 and pad_ok
+            assert np.array_equal(got, want), (c, border, w, h)
+
+
+def test_pyramid_five_levels(kcv, oracle, ctx):
+    rng = np.random.default_rng(9)
+    for (w, h, c) in [(515, 301, 1), (200, 131, 3), (128, 96, 4)]:
+        host = padded(rng, h, w * c, np.uint8, 0)
+        _k, sp, ss = device_image(torch, host)
+        sizes = pyr_sizes(w, h, 5)
+        outs = [device_output(torch, lh, lw * c, np.uint8, 0) for (lw, lh) in sizes]
+        err = kcv.build_pyramid_u8(sp, ss, w, h, c, [o[1] for o in outs], [o[2] for o in outs], 4, ctx)
+        assert err == kcv.OK
+        assert ctx.synchronize() == kcv.OK
+        level = host
+        lw, lh = w, h
+        for (ow, oh), (buf, _p, st) in zip(sizes, outs):
+            e2, want = oracle.blur_and_downsample_u8(level, lw, lh, c, 4)
+            got, _ = read_output(buf, oh, ow * c, np.uint8, st)
+            assert e2 == 0 and np.array_equal(got, want)
+            level, lw, lh = want, ow, oh
+
+
+# ---------------------------------------------------------------------------
+def _kats():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "kats.json")) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.mark.parametrize("case", _kats(), ids=lambda c: c["name"])
+def test_reference_kats_through_c_abi(kcv, oracle, ctx, case):
+    dtype = np.dtype(case["dtype"])
+    host = np.array(case["src"], dtype=dtype)
+    w, h, c = case["width"], case["height"], case["channels"]
+    if case["func"] == "gaussian_blur_u8":
+        got, _ = run_gaussian(kcv, ctx, host, w, h, c, case["kernel_width"], case["sigma_x"], case["border"])
+        err, want = oracle.gaussian_blur_u8(host, w, h, c, case["kernel_width"], case["sigma_x"], case["border"])
+    elif case["func"] == "separable_filter_2d":
+        dt = "u8" if dtype == np.uint8 else "u16"
+        got, _ = run_separable(kcv, ctx, dt, host, w, h, c, case["kernel_x"], case["kernel_y"], case["border"])
+        err, want = oracle.separable_filter_2d(host, w, h, c, np.array(case["kernel_x"], dtype),
+                                               np.array(case["kernel_y"], dtype), case["border"])
+    else:
+        _k, sp, ss = device_image(torch, host)
+        ow, oh = (w + 1) // 2, (h + 1) // 2
+        obuf, dp, ds = device_output(torch, oh, ow * c, np.uint8, 0)
+        assert kcv.blur_and_downsample_u8(sp, ss, w, h, dp, ds, c, case["border"], ctx) == kcv.OK
+        assert ctx.synchronize() == kcv.OK
+        got, _ = read_output(obuf, oh, ow * c, np.uint8, ds)
+        err, want = oracle.blur_and_downsample_u8(host, w, h, c, case["border"])
+    exp = np.array(case["expected"], dtype=np.int64)
+    assert np.abs(got.astype(np.int64) - exp).max() <= case["tolerance"]
+    assert np.array_equal(got, want)  # and bit-exact to the oracle
+
+
+# ---------------------------------------------------------------------------
+# Full-size configurations: bit-exact against the (multithreaded) oracle.
+
+def test_config_hd_gray_binomial5(kcv, oracle, ctx):
+    rng = np.random.default_rng(0)
+    host = padded(rng, 1080, 1920, np.uint8, 64)
+    check_host = host
+    got, pad_ok = run_gaussian(kcv, ctx, check_host, 1920, 1080, 1, 5, 0.0, 1, dst_pad=64)
+    err, want = oracle.gaussian_blur_u8(host, 1920, 1080, 1, 5, 0.0, 1, nthreads=16)
+    assert err == 0 and pad_ok and np.array_equal(got, want)
+
+
+def test_config_4k_rgba_sigma7(kcv, oracle, ctx):
+    rng = np.random.default_rng(1)
+    host = padded(rng, 2160, 3840 * 4, np.uint8, 0)
+    got, pad_ok = run_gaussian(kcv, ctx, host, 3840, 2160, 4, 7, 1.5, 4, dst_pad=0)
+    err, want = oracle.gaussian_blur_u8(host, 3840, 2160, 4, 7, 1.5, 4, nthreads=16)
+    assert err == 0 and pad_ok and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("dt,border", [("u16", 2), ("u16", 3), ("s16", 0)])
+def test_config_4k_separable(kcv, oracle, ctx, dt, border):
+    dtype = SEP_DT[dt]
+    rng = np.random.default_rng(1)
+    host = padded(rng, 2160, 3840, dtype, 0)
+    kx = rng.integers(0, 5, 5)
+    ky = rng.integers(0, 5, 5)
+    bv = 17 if border == 0 else None
+    got, _ = run_separable(kcv, ctx, dt, host, 3840, 2160, 1, kx, ky, border, bv)
+    err, want = oracle.separable_filter_2d(host, 3840, 2160, 1, kx.astype(dtype), ky.astype(dtype), border,
+                                           ext=bv is not None, border_value=bv or 0, nthreads=16)
+    assert err == 0 and np.array_equal(got, want)

@@ -1,0 +1,250 @@
+"""Python binding of the GB300 separable-filter library (libkleidicv_gpu.so).
+
+The product is the C ABI declared in include/kleidicv_gpu.h; this module binds
+it with ctypes so that Python callers (the tests, the benchmark, a serving
+front-end) can drive it with raw device pointers or with torch CUDA tensors.
+Function names, argument order and error codes are those of KleidiCV's C API
+(kleidicv/include/kleidicv/kleidicv.h:2091-2218) plus the trailing context.
+
+There is no CPU fallback: if the shared library is missing, or no sm_103
+device is present, the calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkleidicv_gpu.so")
+
+# kleidicv_error_t (kleidicv/include/kleidicv/ctypes.h:26-41) + GPU extensions
+OK, NOT_IMPLEMENTED, NULL_POINTER, RANGE, ALLOCATION, ALIGNMENT, CONTEXT_MISMATCH = range(7)
+ERROR_CUDA, ERROR_NO_DEVICE, ERROR_TIMEOUT, ERROR_BUSY = 0x100, 0x101, 0x102, 0x103
+# kleidicv_border_type_t (ctypes.h:60-79)
+CONSTANT, REPLICATE, REFLECT, WRAP, REVERSE, TRANSPARENT, NONE = range(7)
+# kleidicv_gpu_op_t
+OP_GAUSSIAN_BLUR_U8, OP_SEPARABLE_U8, OP_SEPARABLE_U16, OP_SEPARABLE_S16, OP_BLUR_AND_DOWNSAMPLE_U8 = range(5)
+
+ERROR_NAMES = {0: "OK", 1: "NOT_IMPLEMENTED", 2: "NULL_POINTER", 3: "RANGE", 4: "ALLOCATION",
+               5: "ALIGNMENT", 6: "CONTEXT_MISMATCH", 0x100: "CUDA", 0x101: "NO_DEVICE",
+               0x102: "TIMEOUT", 0x103: "BUSY"}
+
+_sz, _vp, _f, _i, _u8, _u16, _i16 = (ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
+                                     ctypes.c_uint8, ctypes.c_uint16, ctypes.c_int16)
+
+
+class Request(ctypes.Structure):
+    """kleidicv_gpu_request_t"""
+    _fields_ = [("op", _i), ("src", _vp), ("src_stride", _sz), ("dst", _vp), ("dst_stride", _sz),
+                ("width", _sz), ("height", _sz), ("channels", _sz), ("kernel_width", _sz),
+                ("kernel_height", _sz), ("sigma_x", _f), ("sigma_y", _f),
+                ("kernel_x", ctypes.c_int32 * 5), ("kernel_y", ctypes.c_int32 * 5),
+                ("border_type", _i), ("border_value", ctypes.c_int32),
+                ("allow_extensions", ctypes.c_int32)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pool_limit_bytes", _sz), ("max_inflight_batches", _i), ("max_batch_requests", _i),
+                ("max_queue", _i)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", _i), ("arrival_s", ctypes.c_double),
+                ("admitted_s", ctypes.c_double), ("completed_s", ctypes.c_double)]
+
+
+# name -> (restype, argtypes).  This table is also the list of exported symbols
+# the CPU tests check against include/kleidicv_gpu.h.
+SIGNATURES = {
+    "kleidicv_gpu_context_create": (_i, [ctypes.POINTER(_vp), _i, _vp, _sz]),
+    "kleidicv_gpu_context_destroy": (_i, [_vp]),
+    "kleidicv_gpu_context_set_stream": (_i, [_vp, _vp]),
+    "kleidicv_gpu_context_get_stream": (_vp, [_vp]),
+    "kleidicv_gpu_context_synchronize": (_i, [_vp]),
+    "kleidicv_gpu_context_fail_next_allocations": (None, [_vp, _i]),
+    "kleidicv_gpu_context_launch_count": (ctypes.c_uint64, [_vp]),
+    "kleidicv_gpu_gaussian_blur_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i, _vp]),
+    "kleidicv_gpu_gaussian_blur_u8_ex": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i,
+                                              _u8, _vp]),
+    "kleidicv_gpu_separable_filter_2d_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp, _sz,
+                                                 _i, _vp]),
+    "kleidicv_gpu_separable_filter_2d_u16": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp, _sz,
+                                                  _i, _vp]),
+    "kleidicv_gpu_separable_filter_2d_u8_ex": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp,
+                                                    _sz, _i, _u8, _vp]),
+    "kleidicv_gpu_separable_filter_2d_u16_ex": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp,
+                                                     _sz, _i, _u16, _vp]),
+    "kleidicv_gpu_separable_filter_2d_s16_ex": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp,
+                                                     _sz, _i, _i16, _vp]),
+    "kleidicv_gpu_blur_and_downsample_u8": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _vp]),
+    "kleidicv_gpu_blur_and_downsample_u8_ex": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _u8, _vp]),
+    "kleidicv_gpu_build_pyramid_u8": (_i, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _i, _vp]),
+    "kleidicv_gpu_batch_plan_create": (_i, [ctypes.POINTER(Request), _sz, ctypes.POINTER(_i),
+                                            ctypes.POINTER(_vp), _vp]),
+    "kleidicv_gpu_batch_plan_launch": (_i, [_vp, _i, _vp]),
+    "kleidicv_gpu_batch_plan_destroy": (_i, [_vp]),
+    "kleidicv_gpu_batch_plan_tile_count": (_sz, [_vp]),
+    "kleidicv_gpu_batch_submit": (_i, [ctypes.POINTER(Request), _sz, ctypes.POINTER(_i), _vp]),
+    "kleidicv_gpu_server_create": (_i, [ctypes.POINTER(ServerConfig), _i, ctypes.POINTER(_vp)]),
+    "kleidicv_gpu_server_destroy": (_i, [_vp]),
+    "kleidicv_gpu_server_alloc": (_vp, [_vp, _sz]),
+    "kleidicv_gpu_server_free": (None, [_vp, _vp]),
+    "kleidicv_gpu_server_submit": (_i, [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "kleidicv_gpu_server_poll": (_sz, [_vp, ctypes.POINTER(Completion), _sz, _i]),
+    "kleidicv_gpu_server_now": (ctypes.c_double, [_vp]),
+    "kleidicv_gpu_server_drain": (_i, [_vp]),
+    "kleidicv_gpu_gaussian_half_kernel": (_i, [_sz, _f, ctypes.POINTER(_u8)]),
+}
+
+_lib = None
+
+
+def lib(path: str | None = None) -> ctypes.CDLL:
+    """Loads libkleidicv_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(f"{p} is missing: run build() first (there is no CPU fallback)")
+        l = ctypes.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(l, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def build(force: bool = False) -> str:
+    from importlib import util
+
+    spec = util.spec_from_file_location("_kcv_build", os.path.join(HERE, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def half_kernel(ksize: int, sigma: float):
+    out = (ctypes.c_uint8 * 128)()
+    ok = lib().kleidicv_gpu_gaussian_half_kernel(ksize, sigma, out)
+    return [int(v) for v in out[: ksize // 2 + 1]] if ok else None
+
+
+class Context:
+    """kleidicv_gpu_context_t bound to a device and a CUDA stream handle."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, pool_limit: int = 0):
+        h = ctypes.c_void_p()
+        err = lib().kleidicv_gpu_context_create(ctypes.byref(h), device, stream or None, pool_limit)
+        if err != OK:
+            raise RuntimeError(f"kleidicv_gpu_context_create failed: {ERROR_NAMES.get(err, err)}")
+        self.handle = h
+
+    @classmethod
+    def for_torch(cls, device: int = 0, pool_limit: int = 0):
+        """Context on torch's current stream of `device`."""
+        import torch
+
+        return cls(device, torch.cuda.current_stream(device).cuda_stream, pool_limit)
+
+    def set_stream(self, stream: int | None):
+        lib().kleidicv_gpu_context_set_stream(self.handle, stream or None)
+
+    def synchronize(self) -> int:
+        return lib().kleidicv_gpu_context_synchronize(self.handle)
+
+    def launch_count(self) -> int:
+        return lib().kleidicv_gpu_context_launch_count(self.handle)
+
+    def fail_next_allocations(self, n: int):
+        lib().kleidicv_gpu_context_fail_next_allocations(self.handle, n)
+
+    def close(self):
+        if self.handle:
+            lib().kleidicv_gpu_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _h(ctx):
+    return None if ctx is None else ctx.handle
+
+
+def _k(vals, ctype):
+    if vals is None:
+        return None
+    arr = (ctype * len(vals))(*[int(v) for v in vals])
+    return ctypes.cast(arr, ctypes.c_void_p), arr
+
+
+# --- C-API mirrors (raw pointers and byte strides) -------------------------
+
+def gaussian_blur_u8(src, src_stride, dst, dst_stride, width, height, channels, kernel_width,
+                     kernel_height, sigma_x, sigma_y, border_type, ctx=None, border_value=None):
+    if border_value is None:
+        return lib().kleidicv_gpu_gaussian_blur_u8(src, src_stride, dst, dst_stride, width, height,
+                                                   channels, kernel_width, kernel_height, sigma_x,
+                                                   sigma_y, border_type, _h(ctx))
+    return lib().kleidicv_gpu_gaussian_blur_u8_ex(src, src_stride, dst, dst_stride, width, height,
+                                                  channels, kernel_width, kernel_height, sigma_x,
+                                                  sigma_y, border_type, border_value, _h(ctx))
+
+
+def separable_filter_2d(dtype, src, src_stride, dst, dst_stride, width, height, channels, kernel_x,
+                        kernel_width, kernel_y, kernel_height, border_type, ctx=None,
+                        border_value=None):
+    """dtype: 'u8' | 'u16' | 's16' (s16 exists only as an extension)."""
+    ct = {"u8": ctypes.c_uint8, "u16": ctypes.c_uint16, "s16": ctypes.c_int16}[dtype]
+    kx = _k(kernel_x, ct)
+    ky = _k(kernel_y, ct)
+    kxp = kx[0] if kx else None
+    kyp = ky[0] if ky else None
+    L = lib()
+    if dtype == "s16":
+        return L.kleidicv_gpu_separable_filter_2d_s16_ex(src, src_stride, dst, dst_stride, width, height,
+                                                         channels, kxp, kernel_width, kyp, kernel_height,
+                                                         border_type, border_value or 0, _h(ctx))
+    if border_value is None:
+        fn = getattr(L, f"kleidicv_gpu_separable_filter_2d_{dtype}")
+        return fn(src, src_stride, dst, dst_stride, width, height, channels, kxp, kernel_width, kyp,
+                  kernel_height, border_type, _h(ctx))
+    fn = getattr(L, f"kleidicv_gpu_separable_filter_2d_{dtype}_ex")
+    return fn(src, src_stride, dst, dst_stride, width, height, channels, kxp, kernel_width, kyp,
+              kernel_height, border_type, border_value, _h(ctx))
+
+
+def blur_and_downsample_u8(src, src_stride, src_width, src_height, dst, dst_stride, channels,
+                           border_type, ctx=None, border_value=None):
+    if border_value is None:
+        return lib().kleidicv_gpu_blur_and_downsample_u8(src, src_stride, src_width, src_height, dst,
+                                                         dst_stride, channels, border_type, _h(ctx))
+    return lib().kleidicv_gpu_blur_and_downsample_u8_ex(src, src_stride, src_width, src_height, dst,
+                                                        dst_stride, channels, border_type,
+                                                        border_value, _h(ctx))
+
+
+def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst_strides,
+                     border_type, ctx=None):
+    n = len(dsts)
+    dp = (ctypes.c_void_p * max(n, 1))(*dsts)
+    ds = (ctypes.c_size_t * max(n, 1))(*dst_strides)
+    return lib().kleidicv_gpu_build_pyramid_u8(src, src_stride, src_width, src_height, channels, n,
+                                               ctypes.cast(dp, ctypes.c_void_p),
+                                               ctypes.cast(ds, ctypes.c_void_p), border_type, _h(ctx))
+
+
+# --- torch helpers ---------------------------------------------------------
+
+def ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def stride(t):
+    return 0 if t is None else t.stride(0) * t.element_size()

@@ -1,0 +1,651 @@
+// C-ABI of the GB300 separable-filter library: validation in the reference's
+// order, request preparation (weights, routing, tiling, TMA descriptors) and
+// dispatch onto the context's stream.
+#include <cudaTypedefs.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "host.h"
+#include "tune_table.h"
+
+namespace kcv {
+
+namespace {
+
+constexpr uint64_t kMaxImagePixels = (1ull << 48) - 1;  // kleidicv.h:103
+constexpr size_t kMaxChannels = 4;                      // kleidicv.h:110
+
+bool fixed_border(int b) {
+  return b == BORDER_REPLICATE || b == BORDER_REFLECT || b == BORDER_WRAP || b == BORDER_REVERSE;
+}
+// get_fixed_border_type (workspace/border_types.h:21-35); the _ex entry
+// points additionally accept CONSTANT.
+bool border_supported(int b, bool ext) { return fixed_border(b) || (ext && b == BORDER_CONSTANT); }
+
+// CHECK_IMAGE_SIZE (utils.h:419-430).
+bool image_size_ok(size_t w, size_t h) {
+  size_t n;
+  if (__builtin_mul_overflow(w, h, &n)) return false;
+  return n <= kMaxImagePixels;
+}
+
+// check_pointer_and_stride for 2-byte types (utils.h:379-390).
+bool stride_misaligned(size_t stride, size_t height, size_t elem) {
+  return height > 1 && (stride % elem) != 0;
+}
+
+// gaussian_blur_is_implemented (filters/gaussian_blur.h:38-82).
+bool gaussian_is_implemented(size_t w, size_t h, size_t kw, size_t kh, float sx, float sy,
+                             size_t c, int border, bool ext) {
+  if (kw != kh) return false;
+  if (kw < 3 || kw > 255) return false;
+  if ((kw & 1) != 1) return false;
+  if (!(sx == sy)) return false;
+  if (w < kw - 1 || h < kw - 1) return false;
+  if (c > kMaxChannels) return false;
+  if (kw > 9 && kw != 15 && kw != 21) {
+    if (border != BORDER_REPLICATE && !ext) return false;
+    const size_t margin = kw / 2;
+    const size_t aligned = (margin + 7) / 8 * 8;
+    if (w < aligned + margin) return false;
+  }
+  return true;
+}
+
+int binomial_coef(int k, int i) {
+  static const int c3[] = {1, 2, 1}, c5[] = {1, 4, 6, 4, 1}, c7[] = {2, 7, 14, 18, 14, 7, 2},
+                   c9[] = {4, 13, 30, 51, 60, 51, 30, 13, 4};
+  switch (k) {
+    case 3: return c3[i];
+    case 5: return c5[i];
+    case 7: return c7[i];
+    default: return c9[i];
+  }
+}
+
+void fill_common(FilterJob &j, const void *src, size_t src_stride, void *dst, size_t dst_stride,
+                 size_t w, size_t h, size_t c, int border, int border_value) {
+  memset(&j, 0, sizeof(j));
+  j.src = static_cast<const uint8_t *>(src);
+  j.dst = static_cast<uint8_t *>(dst);
+  j.src_stride = static_cast<int64_t>(src_stride);
+  j.dst_stride = static_cast<int64_t>(dst_stride);
+  j.width = static_cast<int32_t>(w);
+  j.height = static_cast<int32_t>(h);
+  j.channels = static_cast<int32_t>(c);
+  j.out_width = static_cast<int32_t>(w);
+  j.out_height = static_cast<int32_t>(h);
+  j.border = border;
+  j.border_value = border_value;
+}
+
+int elem_size(int mode) { return (mode == MODE_SEP_U16 || mode == MODE_SEP_S16) ? 2 : 1; }
+
+int halo_chunks(const FilterJob &j) {
+  const int halo_elems = j.mode == MODE_BLURDOWN ? 2 * j.channels + 2 : (j.ksize / 2) * j.channels;
+  return (halo_elems * elem_size(j.mode) + kChunk - 1) / kChunk;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+kleidicv_error_t prepare_gaussian(const uint8_t *src, size_t src_stride, uint8_t *dst,
+                                  size_t dst_stride, size_t width, size_t height,
+                                  size_t channels, size_t kernel_width, size_t kernel_height,
+                                  float sigma_x, float sigma_y, int border, bool ext,
+                                  int border_value, Prepared *out) {
+  // gaussian_blur_api.cpp:28-37, then gaussian_blur_checks (gaussian_blur.h:86-95)
+  if (!border_supported(border, ext)) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!gaussian_is_implemented(width, height, kernel_width, kernel_height, sigma_x, sigma_y,
+                               channels, border, ext))
+    return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!src || !dst) return KLEIDICV_ERROR_NULL_POINTER;
+  if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
+
+  *out = Prepared{};
+  if (channels == 0) return KLEIDICV_OK;
+  const int k = static_cast<int>(kernel_width);
+  const bool fixed = k <= 9 || k == 15 || k == 21;
+  if (fixed && k <= 9 && sigma_x == 0.0f) {  // gaussian_blur_fixed_neon.cpp:633-637
+    out->kind = Prepared::FUSED;
+    FilterJob &j = out->fused;
+    fill_common(j, src, src_stride, dst, dst_stride, width, height, channels, border,
+                border_value & 0xFF);
+    j.mode = MODE_BINOM;
+    j.ksize = k;
+    for (int t = 0; t < k; ++t) j.wy[t] = j.wx[t] = binomial_coef(k, t);
+    return KLEIDICV_OK;
+  }
+  uint8_t half[128];
+  if (!gaussian_half_kernel(kernel_width, sigma_x, half)) {
+    out->kind = Prepared::COPY;
+    out->src = src;
+    out->src_stride = src_stride;
+    out->dst = dst;
+    out->dst_stride = dst_stride;
+    out->row_bytes = width * channels;
+    out->rows = height;
+    return KLEIDICV_OK;
+  }
+  const int r = k / 2;
+  int sum = half[r];
+  for (int i = 0; i < r; ++i) sum += 2 * half[i];
+  if (fixed && sum == 256) {
+    out->kind = Prepared::FUSED;
+    FilterJob &j = out->fused;
+    fill_common(j, src, src_stride, dst, dst_stride, width, height, channels, border,
+                border_value & 0xFF);
+    j.mode = MODE_SIGMA;
+    j.ksize = k;
+    for (int t = 0; t < k; ++t) j.wy[t] = j.wx[t] = half[t <= r ? t : k - 1 - t];
+    return KLEIDICV_OK;
+  }
+  out->kind = Prepared::GENERIC;
+  GenericJob &g = out->generic;
+  memset(&g, 0, sizeof(g));
+  g.src = src;
+  g.dst = dst;
+  g.src_stride = static_cast<int64_t>(src_stride);
+  g.dst_stride = static_cast<int64_t>(dst_stride);
+  g.width = static_cast<int32_t>(width);
+  g.height = static_cast<int32_t>(height);
+  g.channels = static_cast<int32_t>(channels);
+  g.border = border;
+  g.border_value = border_value & 0xFF;
+  g.ksize = k;
+  g.arbitrary = fixed ? 0 : 1;
+  g.vert_saturates = (!fixed && width * channels >= 16) ? 1 : 0;
+  g.arb_border_len = static_cast<int32_t>((channels * r + 7) / 8 * 8);
+  memcpy(g.half, half, r + 1);
+  // Vertical result of a column inside a CONSTANT border: sum of all weights
+  // times the border value, rounded like the vertical pass.
+  const uint32_t acc = static_cast<uint32_t>(sum) * (border_value & 0xFF) + 128u;
+  g.v_const = static_cast<int32_t>(g.vert_saturates ? (std::min(acc, 0xFFFFu) >> 8)
+                                                    : ((acc >> 8) & 0xFFu));
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t prepare_separable(int elem, const void *src, size_t src_stride, void *dst,
+                                   size_t dst_stride, size_t width, size_t height,
+                                   size_t channels, const void *kernel_x, size_t kernel_width,
+                                   const void *kernel_y, size_t kernel_height, int border,
+                                   bool ext, int border_value, Prepared *out) {
+  const size_t es = elem == 1 ? 1 : 2;
+  // separable_filter_2d_api.cpp:19-26, then the stripe checks
+  // (separable_filter_2d_neon.cpp:229-235).
+  if (kernel_width != 5 || kernel_height != 5) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (width < kernel_width - 1 || height < kernel_width - 1) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!border_supported(border, ext)) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!src) return KLEIDICV_ERROR_NULL_POINTER;
+  if (stride_misaligned(src_stride, height, es)) return KLEIDICV_ERROR_ALIGNMENT;
+  if (!dst) return KLEIDICV_ERROR_NULL_POINTER;
+  if (stride_misaligned(dst_stride, height, es)) return KLEIDICV_ERROR_ALIGNMENT;
+  if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
+  if (!kernel_x || !kernel_y) return KLEIDICV_ERROR_NULL_POINTER;
+  if (channels > kMaxChannels) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+
+  *out = Prepared{};
+  if (channels == 0) return KLEIDICV_OK;
+  out->kind = Prepared::FUSED;
+  FilterJob &j = out->fused;
+  const int bv = elem == 1 ? (border_value & 0xFF) : (border_value & 0xFFFF);
+  fill_common(j, src, src_stride, dst, dst_stride, width, height, channels, border, bv);
+  j.ksize = 5;
+  j.mode = elem == 1 ? MODE_SEP_U8 : (elem == 2 ? MODE_SEP_U16 : MODE_SEP_S16);
+  for (int t = 0; t < 5; ++t) {
+    if (elem == 1) {
+      j.wx[t] = static_cast<const uint8_t *>(kernel_x)[t];
+      j.wy[t] = static_cast<const uint8_t *>(kernel_y)[t];
+    } else if (elem == 2) {
+      j.wx[t] = static_cast<const uint16_t *>(kernel_x)[t];
+      j.wy[t] = static_cast<const uint16_t *>(kernel_y)[t];
+    } else {
+      j.wx[t] = static_cast<const int16_t *>(kernel_x)[t];
+      j.wy[t] = static_cast<const int16_t *>(kernel_y)[t];
+    }
+  }
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t src_width,
+                                  size_t src_height, uint8_t *dst, size_t dst_stride,
+                                  size_t channels, int border, bool ext, int border_value,
+                                  Prepared *out) {
+  // blur_and_downsample_api.cpp:23-31, then blur_and_downsample_neon.cpp:322-324
+  if (!(src_width >= 4 && src_height >= 4 && channels >= 1 && channels <= kMaxChannels))
+    return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!border_supported(border, ext)) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!src || !dst) return KLEIDICV_ERROR_NULL_POINTER;
+  if (!image_size_ok(src_width, src_height)) return KLEIDICV_ERROR_RANGE;
+
+  *out = Prepared{};
+  out->kind = Prepared::FUSED;
+  FilterJob &j = out->fused;
+  fill_common(j, src, src_stride, dst, dst_stride, src_width, src_height, channels, border,
+              border_value & 0xFF);
+  j.out_width = static_cast<int32_t>((src_width + 1) / 2);
+  j.out_height = static_cast<int32_t>((src_height + 1) / 2);
+  j.mode = MODE_BLURDOWN;
+  j.ksize = 5;
+  for (int t = 0; t < 5; ++t) j.wy[t] = j.wx[t] = binomial_coef(5, t);
+  return KLEIDICV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tiling.
+TileShape tile_shape_for(const FilterJob &j, int sm_count) {
+  const int es = elem_size(j.mode);
+  const long wcb = static_cast<long>(j.width) * j.channels * es;
+  TileShape t{};
+  // Autotuned shapes (committed table) win when present.
+  if (lookup_tile_shape(j.mode, j.ksize, j.channels, wcb, j.out_height, &t.threads, &t.tile_rows,
+                        &t.stage_rows, &t.stages))
+    return t;
+  const int hc = halo_chunks(j);
+  const long chunks = (wcb + kChunk - 1) / kChunk;  // 16-byte chunks per source row
+  const int wi = 32 - 2 * hc;                        // interior chunks per consumer warp
+  int warps = static_cast<int>(std::min<long>(4, std::max<long>(1, (chunks + wi - 1) / wi)));
+  t.threads = 32 * (warps + 1);
+  const long strip_chunks = static_cast<long>(warps) * wi;
+  const long strips = j.mode == MODE_BLURDOWN
+                          ? (static_cast<long>(j.out_width) * j.channels + strip_chunks * 8 - 1) /
+                                (strip_chunks * 8)
+                          : (chunks + strip_chunks - 1) / strip_chunks;
+  const long target = 3L * std::max(sm_count, 1);
+  long bands = std::max(1L, target / std::max(strips, 1L));
+  int rows = static_cast<int>((j.out_height + bands - 1) / bands);
+  rows = std::max(8, std::min(rows, 512));
+  t.tile_rows = rows;
+  t.stage_rows = 4;
+  t.stages = 8;
+  return t;
+}
+
+// Ring depth rule: stages * stage_rows >= K - 1 + 2 * stage_rows, so that a
+// consumer warp never waits for a stage that cannot be issued until a warp
+// behind it releases one; both counts are powers of two.
+static void fix_ring(FilterJob &j) {
+  auto pow2 = [](int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+  };
+  j.stage_rows = std::max(1, std::min(pow2(j.stage_rows), 64));
+  const int k_rows = j.mode == MODE_BLURDOWN ? 5 : j.ksize;
+  int ns = pow2(std::max(2, j.stages));
+  while (ns * j.stage_rows < k_rows - 1 + 2 * j.stage_rows) ns <<= 1;
+  j.stages = ns;
+}
+
+void apply_tile_shape(FilterJob &j, const TileShape &t) {
+  const int es = elem_size(j.mode);
+  const long wcb = static_cast<long>(j.width) * j.channels * es;
+  j.threads = t.threads;
+  j.tile_rows = t.tile_rows;
+  j.stage_rows = t.stage_rows;
+  j.stages = t.stages;
+  fix_ring(j);
+  j.halo_chunks = halo_chunks(j);
+  // Consumer warps x interior chunks per warp (one producer warp on top).
+  const int interior = (j.threads / 32 - 1) * (32 - 2 * j.halo_chunks);
+  // Row bands: gridDim.y is limited to 65535.
+  if ((j.out_height + j.tile_rows - 1) / j.tile_rows > 65535)
+    j.tile_rows = (j.out_height + 65534) / 65535;
+  if (j.mode == MODE_BLURDOWN) {
+    j.strip_out_bytes = interior * 8;
+    j.strips = static_cast<int32_t>(
+        (static_cast<long>(j.out_width) * j.channels + j.strip_out_bytes - 1) / j.strip_out_bytes);
+  } else {
+    j.strip_out_bytes = interior * kChunk;
+    j.strips = static_cast<int32_t>((wcb + j.strip_out_bytes - 1) / j.strip_out_bytes);
+  }
+  j.row_tiles = (j.out_height + j.tile_rows - 1) / j.tile_rows;
+}
+
+void plan_fused(FilterJob &j, int sm_count) { apply_tile_shape(j, tile_shape_for(j, sm_count)); }
+
+void encode_tma(FilterJob &j) {
+  j.use_tma = 0;
+  j.box_lbw = 8;
+  const long wcb = static_cast<long>(j.width) * j.channels * elem_size(j.mode);
+  if ((reinterpret_cast<uintptr_t>(j.src) & 15) != 0 || (j.src_stride & 15) != 0) return;
+  if (wcb < 256 || j.height < 1 || j.stage_rows > 256) return;
+  auto encode = tensor_map_encoder();
+  if (!encode) return;
+  // Rows that are a whole number of 8-byte units are viewed as u64 elements so
+  // that one box spans 2048 bytes (one TMA per stage for a 4-warp strip).
+  const bool wide = (wcb % 8) == 0;
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(j.src_stride)};
+  const cuuint32_t estr[2] = {1u, 1u};
+  auto enc = [&](CUtensorMap *m, bool w, cuuint32_t rows) {
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(w ? wcb / 8 : wcb),
+                                static_cast<cuuint64_t>(j.height)};
+    const cuuint32_t box[2] = {256u, rows};
+    return encode(m, w ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                  const_cast<uint8_t *>(j.src), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+  };
+  const cuuint32_t rb = static_cast<cuuint32_t>(j.stage_rows);
+  if (!enc(&j.tmap, wide, rb) || !enc(&j.tmap_row, wide, 1u) || !enc(&j.tmap_wrap, false, rb) ||
+      !enc(&j.tmap_wrap_row, false, 1u))
+    return;
+  j.box_lbw = wide ? 11 : 8;
+  j.use_tma = 1;
+}
+
+// ---------------------------------------------------------------------------
+// Context plumbing.
+kleidicv_error_t cuda_status(kleidicv_gpu_context *ctx, cudaError_t e) {
+  if (e == cudaSuccess) return KLEIDICV_OK;
+  if (ctx) ctx->last_cuda_error = e;
+  return KLEIDICV_GPU_ERROR_CUDA;
+}
+
+void *ctx_alloc(kleidicv_gpu_context *ctx, size_t bytes) {
+  int f = ctx->fail_allocs.load();
+  while (f > 0) {
+    if (ctx->fail_allocs.compare_exchange_weak(f, f - 1)) return nullptr;
+  }
+  if (ctx->pool_used.load() + bytes > ctx->pool_limit) return nullptr;
+  void *p = nullptr;
+  if (cudaMallocAsync(&p, bytes, ctx->stream) != cudaSuccess) return nullptr;
+  ctx->pool_used += bytes;
+  return p;
+}
+
+void ctx_free(kleidicv_gpu_context *ctx, void *p, size_t bytes) {
+  if (!p) return;
+  cudaFreeAsync(p, ctx->stream);
+  ctx->pool_used -= bytes;
+}
+
+namespace {
+thread_local kleidicv_gpu_context *t_default_ctx = nullptr;
+}
+
+kleidicv_error_t resolve_context(kleidicv_gpu_context *&ctx) {
+  if (ctx) return KLEIDICV_OK;
+  if (!t_default_ctx) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return KLEIDICV_GPU_ERROR_NO_DEVICE;
+    kleidicv_error_t e = kleidicv_gpu_context_create(&t_default_ctx, dev, nullptr, 0);
+    if (e != KLEIDICV_OK) return e;
+  }
+  ctx = t_default_ctx;
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
+  switch (p.kind) {
+    case Prepared::NOTHING:
+      return KLEIDICV_OK;
+    case Prepared::COPY:
+      return cuda_status(ctx, cudaMemcpy2DAsync(p.dst, p.dst_stride, p.src, p.src_stride,
+                                                p.row_bytes, p.rows, cudaMemcpyDeviceToDevice,
+                                                ctx->stream));
+    case Prepared::FUSED: {
+      plan_fused(p.fused, ctx->sm_count);
+      encode_tma(p.fused);
+      cudaError_t e = launch_fused(p.fused, ctx->d_err, ctx->stream);
+      ctx->launches += 1;
+      return cuda_status(ctx, e);
+    }
+    case Prepared::GENERIC: {
+      const GenericJob &g = p.generic;
+      const size_t vstride = (static_cast<size_t>(g.width) * g.channels + 15) / 16 * 16;
+      const size_t bytes = vstride * g.height;
+      uint8_t *scratch = static_cast<uint8_t *>(ctx_alloc(ctx, bytes));
+      if (!scratch) return KLEIDICV_ERROR_ALLOCATION;
+      cudaError_t e = launch_generic_gaussian(g, scratch, vstride, ctx->stream);
+      ctx->launches += 2;
+      ctx_free(ctx, scratch, bytes);
+      return cuda_status(ctx, e);
+    }
+  }
+  return KLEIDICV_OK;
+}
+
+}  // namespace kcv
+
+// ===========================================================================
+// C ABI
+using namespace kcv;
+
+extern "C" {
+
+kleidicv_error_t kleidicv_gpu_context_create(kleidicv_gpu_context_t **out, int device,
+                                             void *stream, size_t pool_limit_bytes) {
+  if (!out) return KLEIDICV_ERROR_NULL_POINTER;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+    return KLEIDICV_GPU_ERROR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return KLEIDICV_GPU_ERROR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return KLEIDICV_GPU_ERROR_NO_DEVICE;  // sm_103 only
+  DeviceGuard guard(device);
+  auto *ctx = new kleidicv_gpu_context();
+  ctx->device = device;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  ctx->pool_limit = pool_limit_bytes ? pool_limit_bytes : (40ull << 30);
+  ctx->sm_count = prop.multiProcessorCount;
+  if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) {
+    delete ctx;
+    return KLEIDICV_GPU_ERROR_CUDA;
+  }
+  *out = ctx;
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx) {
+  if (!ctx) return KLEIDICV_ERROR_NULL_POINTER;
+  DeviceGuard guard(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_err);
+  delete ctx;
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t kleidicv_gpu_context_set_stream(kleidicv_gpu_context_t *ctx, void *stream) {
+  if (!ctx) return KLEIDICV_ERROR_NULL_POINTER;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return KLEIDICV_OK;
+}
+
+void *kleidicv_gpu_context_get_stream(const kleidicv_gpu_context_t *ctx) {
+  return ctx ? static_cast<void *>(ctx->stream) : nullptr;
+}
+
+kleidicv_error_t kleidicv_gpu_context_synchronize(kleidicv_gpu_context_t *ctx) {
+  if (resolve_context(ctx) != KLEIDICV_OK) return KLEIDICV_GPU_ERROR_NO_DEVICE;
+  DeviceGuard guard(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e);
+  int flag = 0;
+  e = cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(ctx, e);
+  if (flag) {
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    return KLEIDICV_GPU_ERROR_TIMEOUT;
+  }
+  if (ctx->last_cuda_error != cudaSuccess) {
+    ctx->last_cuda_error = cudaSuccess;
+    return KLEIDICV_GPU_ERROR_CUDA;
+  }
+  return KLEIDICV_OK;
+}
+
+void kleidicv_gpu_context_fail_next_allocations(kleidicv_gpu_context_t *ctx, int count) {
+  if (ctx) ctx->fail_allocs = count;
+}
+
+uint64_t kleidicv_gpu_context_launch_count(const kleidicv_gpu_context_t *ctx) {
+  return ctx ? ctx->launches.load() : 0;
+}
+
+static kleidicv_error_t run(kleidicv_gpu_context_t *ctx, kleidicv_error_t prep, Prepared &p) {
+  if (prep != KLEIDICV_OK) return prep;
+  if (p.kind == Prepared::NOTHING) return KLEIDICV_OK;
+  kleidicv_error_t e = resolve_context(ctx);
+  if (e != KLEIDICV_OK) return e;
+  DeviceGuard guard(ctx->device);
+  return execute(ctx, p);
+}
+
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8(const uint8_t *src, size_t src_stride, uint8_t *dst,
+                                               size_t dst_stride, size_t width, size_t height,
+                                               size_t channels, size_t kernel_width,
+                                               size_t kernel_height, float sigma_x,
+                                               float sigma_y, kleidicv_border_type_t border_type,
+                                               kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_gaussian(src, src_stride, dst, dst_stride, width, height, channels,
+                            kernel_width, kernel_height, sigma_x, sigma_y, border_type, false, 0,
+                            &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8_ex(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height, float sigma_x,
+    float sigma_y, kleidicv_border_type_t border_type, uint8_t border_value,
+    kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_gaussian(src, src_stride, dst, dst_stride, width, height, channels,
+                            kernel_width, kernel_height, sigma_x, sigma_y, border_type, true,
+                            border_value, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint8_t *kernel_x, size_t kernel_width,
+    const uint8_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_separable(1, src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_x, kernel_width, kernel_y, kernel_height, border_type, false,
+                             0, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u16(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint16_t *kernel_x, size_t kernel_width,
+    const uint16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_separable(2, src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_x, kernel_width, kernel_y, kernel_height, border_type, false,
+                             0, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u8_ex(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint8_t *kernel_x, size_t kernel_width,
+    const uint8_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    uint8_t border_value, kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_separable(1, src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_x, kernel_width, kernel_y, kernel_height, border_type, true,
+                             border_value, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u16_ex(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint16_t *kernel_x, size_t kernel_width,
+    const uint16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    uint16_t border_value, kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_separable(2, src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_x, kernel_width, kernel_y, kernel_height, border_type, true,
+                             border_value, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_s16_ex(
+    const int16_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const int16_t *kernel_x, size_t kernel_width,
+    const int16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    int16_t border_value, kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_separable(3, src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_x, kernel_width, kernel_y, kernel_height, border_type, true,
+                             static_cast<uint16_t>(border_value), &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8(const uint8_t *src, size_t src_stride,
+                                                     size_t src_width, size_t src_height,
+                                                     uint8_t *dst, size_t dst_stride,
+                                                     size_t channels,
+                                                     kleidicv_border_type_t border_type,
+                                                     kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_blurdown(src, src_stride, src_width, src_height, dst, dst_stride, channels,
+                            border_type, false, 0, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8_ex(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height, uint8_t *dst,
+    size_t dst_stride, size_t channels, kleidicv_border_type_t border_type, uint8_t border_value,
+    kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_blurdown(src, src_stride, src_width, src_height, dst, dst_stride, channels,
+                            border_type, true, border_value, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_build_pyramid_u8(const uint8_t *src, size_t src_stride,
+                                               size_t src_width, size_t src_height,
+                                               size_t channels, size_t levels,
+                                               uint8_t *const *dst, const size_t *dst_strides,
+                                               kleidicv_border_type_t border_type,
+                                               kleidicv_gpu_context_t *ctx) {
+  if (levels == 0) return KLEIDICV_OK;
+  if (!dst || !dst_strides) return KLEIDICV_ERROR_NULL_POINTER;
+  Prepared p[64];
+  if (levels > 64) return KLEIDICV_ERROR_RANGE;
+  const uint8_t *s = src;
+  size_t ss = src_stride, w = src_width, h = src_height;
+  for (size_t l = 0; l < levels; ++l) {
+    kleidicv_error_t e = prepare_blurdown(s, ss, w, h, dst[l], dst_strides[l], channels,
+                                          border_type, false, 0, &p[l]);
+    if (e != KLEIDICV_OK) return e;
+    s = dst[l];
+    ss = dst_strides[l];
+    w = (w + 1) / 2;
+    h = (h + 1) / 2;
+  }
+  kleidicv_error_t e = resolve_context(ctx);
+  if (e != KLEIDICV_OK) return e;
+  DeviceGuard guard(ctx->device);
+  for (size_t l = 0; l < levels; ++l) {
+    e = execute(ctx, p[l]);
+    if (e != KLEIDICV_OK) return e;
+  }
+  return KLEIDICV_OK;
+}
+
+}  // extern "C"

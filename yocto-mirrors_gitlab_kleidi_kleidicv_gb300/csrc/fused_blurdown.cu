@@ -1,0 +1,22 @@
+#include "fused_inst.cuh"
+namespace kcv {
+bool launch_fused_blurdown(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out) {
+  if (j.mode != MODE_BLURDOWN) return false;
+  return dispatch_channels<MODE_BLURDOWN, 5>(j, e, s, out);
+}
+size_t fused_smem_bytes(const FilterJob &job) {
+  switch (job.mode) {
+    case MODE_SEP_U16: return smem_layout<MODE_SEP_U16>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages).total;
+    default: return smem_layout<MODE_SIGMA>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages).total;
+  }
+}
+cudaError_t launch_fused(const FilterJob &job, int *err, cudaStream_t s) {
+  cudaError_t out = cudaErrorInvalidValue;
+  if (launch_fused_binom(job, err, s, &out) || launch_fused_sigma_small(job, err, s, &out) ||
+      launch_fused_sigma_9(job, err, s, &out) || launch_fused_sigma_15(job, err, s, &out) ||
+      launch_fused_sigma_21(job, err, s, &out) || launch_fused_sep(job, err, s, &out) ||
+      launch_fused_blurdown(job, err, s, &out))
+    return out;
+  return cudaErrorInvalidValue;
+}
+}  // namespace kcv

@@ -1,0 +1,137 @@
+// Generic two-pass Gaussian for arbitrary odd kernel sizes (11..255, the
+// reference's kleidicv/src/filters/gaussian_blur_arbitrary_neon.cpp) and for
+// any generated kernel whose weights do not sum to 256.
+//
+// Pass 1 writes the u8 vertical intermediate of the whole image into a
+// scratch image; pass 2 stages each row segment (plus its border-mapped halo)
+// in shared memory and applies the horizontal taps.  Arithmetic is per
+// element in 32 bits and reproduces, element by element, which rounding the
+// reference applied: the arbitrary-size vector paths add the rounding
+// constant with saturation (vqaddq_u16, :193-194, :306-307), its border
+// vector paths narrow with vrshrn (:340, :374) and its scalar paths cast a
+// u32 sum to u8 (:232-244, :381-383); these differ only when a sum of weights
+// above 256 lets a 16-bit accumulator pass 65535.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "launch.h"
+#include "sepfused.cuh"
+
+namespace kcv {
+
+namespace {
+
+__device__ __forceinline__ uint32_t round_wrap(uint32_t acc) { return ((acc + 128u) >> 8) & 0xFFu; }
+__device__ __forceinline__ uint32_t round_sat(uint32_t acc) {
+  const uint32_t a = acc + 128u;
+  return (a > 0xFFFFu ? 0xFFFFu : a) >> 8;
+}
+
+__device__ __forceinline__ uint32_t weight(const GenericJob &j, int t) {
+  const int r = j.ksize / 2;
+  return j.half[t <= r ? t : j.ksize - 1 - t];
+}
+
+constexpr int kRowsPerThread = 16;
+constexpr int kHThreads = 256;
+constexpr int kHElems = 4 * kHThreads;  // row elements per CTA in pass 2
+
+__global__ void __launch_bounds__(256) generic_vertical(const __grid_constant__ GenericJob j,
+                                                        uint8_t *vbuf, size_t vstride) {
+  const long wc = static_cast<long>(j.width) * j.channels;
+  const long x = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
+  if (x >= wc) return;
+  const int ne = static_cast<int>(wc - x < 4 ? wc - x : 4);
+  const int y0 = blockIdx.y * kRowsPerThread;
+  const int y1 = min(y0 + kRowsPerThread, j.height);
+  const int r = j.ksize / 2;
+  for (int y = y0; y < y1; ++y) {
+    uint32_t acc[4] = {0, 0, 0, 0};
+    for (int t = 0; t < j.ksize; ++t) {
+      const int ry = map_index(y + t - r, j.height, j.border);
+      const uint32_t g = weight(j, t);
+      if (ry < 0) {
+        const uint32_t bv = static_cast<uint32_t>(j.border_value) & 0xFFu;
+        for (int e = 0; e < 4; ++e) acc[e] += g * bv;
+      } else {
+        const uint8_t *row = j.src + static_cast<int64_t>(ry) * j.src_stride + x;
+        if (ne == 4 && (reinterpret_cast<uintptr_t>(row) & 3) == 0) {
+          const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(row));
+          acc[0] += g * (w & 0xFFu);
+          acc[1] += g * ((w >> 8) & 0xFFu);
+          acc[2] += g * ((w >> 16) & 0xFFu);
+          acc[3] += g * (w >> 24);
+        } else {
+          for (int e = 0; e < ne; ++e) acc[e] += g * __ldg(row + e);
+        }
+      }
+    }
+    uint8_t *out = vbuf + static_cast<int64_t>(y) * vstride + x;
+    for (int e = 0; e < ne; ++e)
+      out[e] = static_cast<uint8_t>(j.vert_saturates ? round_sat(acc[e]) : round_wrap(acc[e]));
+  }
+}
+
+__device__ __forceinline__ bool h_saturates(const GenericJob &j, long x, long wc) {
+  if (!j.arbitrary) return false;
+  const long bl = j.arb_border_len;
+  if (wc <= 2 * bl || x < bl || x >= wc - bl) return false;
+  return wc - 2 * bl >= 16;
+}
+
+__global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_constant__ GenericJob j,
+                                                                const uint8_t *vbuf,
+                                                                size_t vstride) {
+  extern __shared__ uint8_t seg[];
+  const int c = j.channels;
+  const int r = j.ksize / 2;
+  const long wc = static_cast<long>(j.width) * c;
+  const int y = blockIdx.y;
+  const long x0 = static_cast<long>(blockIdx.x) * kHElems;
+  const int halo = r * c;
+  const int seg_len = kHElems + 2 * halo;
+  const uint8_t *vrow = vbuf + static_cast<int64_t>(y) * vstride;
+  // Stage [x0 - halo, x0 + kHElems + halo) with the border resolved per element.
+  for (int i = threadIdx.x; i < seg_len; i += blockDim.x) {
+    const long xe = x0 - halo + i;
+    uint8_t v;
+    if (xe >= 0 && xe < wc) {
+      v = vrow[xe];
+    } else {
+      const long col = xe >= 0 ? xe / c : -((-xe + c - 1) / c);
+      const int ch = static_cast<int>(xe - col * c);
+      const int mc = map_index(static_cast<int>(col), j.width, j.border);
+      v = mc < 0 ? static_cast<uint8_t>(j.v_const) : vrow[static_cast<long>(mc) * c + ch];
+    }
+    seg[i] = v;
+  }
+  __syncthreads();
+  uint8_t *drow = j.dst + static_cast<int64_t>(y) * j.dst_stride;
+  for (int k = 0; k < 4; ++k) {
+    const int local = threadIdx.x * 4 + k;
+    const long x = x0 + local;
+    if (x >= wc) break;
+    uint32_t acc = 0;
+    for (int t = 0; t < j.ksize; ++t) acc += weight(j, t) * seg[local + t * c];
+    drow[x] = static_cast<uint8_t>(h_saturates(j, x, wc) ? round_sat(acc) : round_wrap(acc));
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch, size_t scratch_stride,
+                                    cudaStream_t stream) {
+  const long wc = static_cast<long>(job.width) * job.channels;
+  const long words = (wc + 3) / 4;
+  dim3 g1(static_cast<unsigned>((words + 255) / 256),
+          static_cast<unsigned>((job.height + kRowsPerThread - 1) / kRowsPerThread));
+  generic_vertical<<<g1, 256, 0, stream>>>(job, scratch, scratch_stride);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t smem = kHElems + 2 * static_cast<size_t>(job.ksize / 2) * job.channels;
+  dim3 g2(static_cast<unsigned>((wc + kHElems - 1) / kHElems), static_cast<unsigned>(job.height));
+  generic_horizontal<<<g2, kHThreads, smem, stream>>>(job, scratch, scratch_stride);
+  return cudaGetLastError();
+}
+
+}  // namespace kcv

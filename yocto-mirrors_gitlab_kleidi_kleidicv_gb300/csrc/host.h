@@ -1,0 +1,96 @@
+// Host-side internals shared by the C-ABI, batch and serving layers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "../../include/kleidicv_gpu.h"
+#include "kcv_job.h"
+#include "launch.h"
+
+struct kleidicv_gpu_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t pool_limit = 0;
+  std::atomic<size_t> pool_used{0};
+  std::atomic<int> fail_allocs{0};
+  std::atomic<uint64_t> launches{0};
+  int *d_err = nullptr;  // device flag kernels set on a bounded-wait timeout
+  int sm_count = 0;
+  cudaError_t last_cuda_error = cudaSuccess;
+};
+
+namespace kcv {
+
+bool gaussian_half_kernel(size_t ksize, float sigma, uint8_t *half);
+
+// Tile shape of the fused kernel for one (mode, size, channels, image size).
+struct TileShape {
+  int threads, tile_rows, stage_rows, stages;
+};
+
+// A validated request, ready to be enqueued.
+struct Prepared {
+  enum Kind { NOTHING, COPY, FUSED, GENERIC } kind = NOTHING;
+  FilterJob fused;
+  GenericJob generic;
+  // COPY (all weight in the centre tap: gaussian_blur_fixed_neon.cpp:565-573)
+  const void *src = nullptr;
+  size_t src_stride = 0;
+  void *dst = nullptr;
+  size_t dst_stride = 0;
+  size_t row_bytes = 0, rows = 0;
+};
+
+kleidicv_error_t prepare_gaussian(const uint8_t *src, size_t src_stride, uint8_t *dst,
+                                  size_t dst_stride, size_t width, size_t height,
+                                  size_t channels, size_t kernel_width, size_t kernel_height,
+                                  float sigma_x, float sigma_y, int border, bool ext,
+                                  int border_value, Prepared *out);
+
+// elem: 1 (u8), 2 (u16), 3 (s16).
+kleidicv_error_t prepare_separable(int elem, const void *src, size_t src_stride, void *dst,
+                                   size_t dst_stride, size_t width, size_t height,
+                                   size_t channels, const void *kernel_x, size_t kernel_width,
+                                   const void *kernel_y, size_t kernel_height, int border,
+                                   bool ext, int border_value, Prepared *out);
+
+kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t src_width,
+                                  size_t src_height, uint8_t *dst, size_t dst_stride,
+                                  size_t channels, int border, bool ext, int border_value,
+                                  Prepared *out);
+
+// Chooses the tile shape (autotune table, else heuristic) and fills the
+// derived tiling fields of a FUSED job.  sm_count sizes the grid.
+void plan_fused(FilterJob &j, int sm_count);
+TileShape tile_shape_for(const FilterJob &j, int sm_count);
+void apply_tile_shape(FilterJob &j, const TileShape &t);
+// Builds the TMA descriptor when the source allows it; sets j.use_tma.
+void encode_tma(FilterJob &j);
+
+// Enqueues a prepared request on ctx's stream.
+kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p);
+
+// Context helpers.
+kleidicv_error_t resolve_context(kleidicv_gpu_context *&ctx);
+void *ctx_alloc(kleidicv_gpu_context *ctx, size_t bytes);
+void ctx_free(kleidicv_gpu_context *ctx, void *p, size_t bytes);
+kleidicv_error_t cuda_status(kleidicv_gpu_context *ctx, cudaError_t e);
+
+// Device guard: makes ctx->device current for the calling thread.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    else prev = -1;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace kcv

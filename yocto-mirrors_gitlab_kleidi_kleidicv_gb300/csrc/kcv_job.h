@@ -1,0 +1,88 @@
+// Host/device shared description of one filter job (one image, one op).
+#pragma once
+
+#include <cuda.h>
+#include <stdint.h>
+
+namespace kcv {
+
+// What the fused stencil computes; selects the arithmetic of both passes.
+enum Mode : int32_t {
+  MODE_BINOM = 0,       // gaussian_blur_u8, sigma == 0 and size <= 9: u16-exact
+  MODE_SIGMA = 1,       // gaussian_blur_u8 with generated weights summing to 256
+  MODE_SIGMA_SAFE = 2,  // generated weights not summing to 256 (per-element path)
+  MODE_SEP_U8 = 3,      // separable_filter_2d_u8, 5x5, saturating
+  MODE_SEP_U16 = 4,     // separable_filter_2d_u16, 5x5, saturating
+  MODE_SEP_S16 = 5,     // separable_filter_2d_s16 (extension)
+  MODE_BLURDOWN = 6,    // blur_and_downsample_u8
+};
+
+// Border codes: the kleidicv_border_type_t values.
+enum Border : int32_t {
+  BORDER_CONSTANT = 0,
+  BORDER_REPLICATE = 1,
+  BORDER_REFLECT = 2,
+  BORDER_WRAP = 3,
+  BORDER_REVERSE = 4,
+};
+
+constexpr int kMaxTaps = 21;  // largest fused kernel size
+constexpr int kChunk = 16;    // bytes of one row owned by one thread
+
+struct FilterJob {
+  // TMA views of src (valid when use_tma).  The span maps count the row in
+  // units of 1 << (box_lbw - 8) bytes (1, or 8 when rows are a multiple of 8
+  // bytes) so that a 256-unit box is 1 << box_lbw bytes wide; the wrap maps
+  // count bytes.  Boxes are stage_rows high, or one row for the *_row maps.
+  CUtensorMap tmap;
+  CUtensorMap tmap_row;
+  CUtensorMap tmap_wrap;
+  CUtensorMap tmap_wrap_row;
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride;  // bytes
+  int64_t dst_stride;  // bytes
+  int32_t width, height, channels;  // source size in pixels
+  int32_t out_width, out_height;    // destination size in pixels
+  int32_t border;
+  int32_t border_value;
+  int32_t mode;
+  int32_t ksize;
+  int32_t use_tma;
+  // Taps of the full kernel: wy vertical, wx horizontal.
+  int32_t wy[kMaxTaps];
+  int32_t wx[kMaxTaps];
+  // Arbitrary-size Gaussian (MODE_SIGMA_SAFE only): reproduces which of the
+  // reference's vector / scalar paths handled each element.
+  int32_t arbitrary;
+  int32_t vert_saturates;
+  int32_t arb_border_len;
+  // Tiling (see plan_tiles): threads per CTA, rows per tile, rows per TMA
+  // stage, stages in the ring, halo chunks per side, strips across a row.
+  int32_t threads;
+  int32_t tile_rows;
+  int32_t stage_rows;
+  int32_t stages;
+  int32_t halo_chunks;
+  int32_t strips;
+  int32_t row_tiles;
+  int32_t strip_out_bytes;  // destination bytes produced per strip
+  int32_t box_lbw;          // log2 of the span box width in bytes (8 or 11)
+};
+
+// Generic per-element Gaussian (any odd size up to 255).
+struct GenericJob {
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride, dst_stride;
+  int32_t width, height, channels;
+  int32_t border, border_value;
+  int32_t ksize;
+  int32_t arbitrary;       // reproduce the arbitrary-size path's rounding choices
+  int32_t vert_saturates;  // arbitrary path: width*channels >= 16
+  int32_t arb_border_len;  // arbitrary path: ceil8(channels * (ksize / 2))
+  int32_t v_const;         // vertical result of a column lying in a CONSTANT border
+  uint8_t half[128];       // half kernel, half[ksize/2] is the centre weight
+};
+
+}  // namespace kcv

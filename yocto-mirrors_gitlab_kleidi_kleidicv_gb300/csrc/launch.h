@@ -1,0 +1,35 @@
+// Host-side launch interface of the device kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kcv_job.h"
+
+namespace kcv {
+
+// Dynamic shared memory the fused kernel needs for `job`'s tiling.
+size_t fused_smem_bytes(const FilterJob &job);
+
+// Launches the fused stencil for job.mode / job.ksize / job.channels on
+// grid (job.strips, job.row_tiles).  Returns cudaErrorInvalidValue when no
+// instantiation exists for the combination.
+cudaError_t launch_fused(const FilterJob &job, int *err_flag, cudaStream_t stream);
+
+// Per-family dispatchers (one translation unit each); return false if the
+// (mode, ksize, channels) combination is not theirs.
+bool launch_fused_binom(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_sigma_small(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_sigma_9(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_sigma_15(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_sigma_21(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+
+// Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
+// generated kernel whose weights do not sum to 256).  `scratch` holds the
+// u8 intermediate image: width*channels bytes per row, `scratch_stride`
+// bytes apart, `height` rows.
+cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch,
+                                    size_t scratch_stride, cudaStream_t stream);
+
+}  // namespace kcv

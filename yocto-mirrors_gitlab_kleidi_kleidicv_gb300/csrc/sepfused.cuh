@@ -1,0 +1,971 @@
+// Fused row-streaming separable stencil for sm_103a.
+//
+// One CTA owns a vertical strip of the image (threads x 16-byte chunks of a
+// row, the outer HC chunks on each side being the horizontal filter halo)
+// and walks down a band of rows:
+//
+//   * rows reach shared memory through a ring of TMA stages
+//     (cp.async.bulk.tensor.2d + mbarrier transaction counts) whenever the
+//     source is 16-byte aligned.  The border is resolved in the address
+//     calculation, never by a padded copy: a stage that reaches above or
+//     below the image loads the border-mapped source rows as single-row
+//     boxes, a WRAP border on an edge strip adds one box from the far end of
+//     the row, and chunks hanging over the left/right edge gather their
+//     mapped elements from shared memory.  Sources that TMA cannot address
+//     (unaligned base or stride) are read with plain loads instead;
+//   * each thread keeps the last K rows of its chunk in registers (a sliding
+//     window rotated by unrolling, so no register moves), and computes the
+//     vertical pass on packed 16-bit lanes in the reference's intermediate
+//     width and rounding;
+//   * the vertical row goes to a double-buffered shared row, one barrier,
+//     then the horizontal pass reads its neighbours' lanes at compile-time
+//     offsets (tap distance = channels elements) and the result is stored
+//     with 16-byte stores.
+//
+// Every output byte equals the reference's: the arithmetic per mode follows
+// kleidicv/src/filters/gaussian_blur_fixed_neon.cpp (binomial 3/5/7/9 and
+// generated-sigma kernels), separable_filter_2d_neon.cpp (u8/u16 saturation)
+// and blur_and_downsample_neon.cpp, with the border offset tables of
+// kleidicv/include/kleidicv/workspace/border_*.h restated as a single-fold
+// index map.
+#pragma once
+
+#include <stdint.h>
+
+#include <type_traits>
+#include <utility>
+
+#include "kcv_job.h"
+#include "ptx.cuh"
+
+namespace kcv {
+
+// ---------------------------------------------------------------------------
+// Compile-time loop: calls f(std::integral_constant<int, I>) for I in [B, E).
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F &&f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + 1, E>(f);
+  }
+}
+
+constexpr int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+template <int MODE>
+struct ModeTraits {
+  static constexpr int ES = (MODE == MODE_SEP_U16 || MODE == MODE_SEP_S16) ? 2 : 1;
+  static constexpr bool LANES = ES == 1;  // u8 data held as packed 16-bit lanes
+};
+
+template <int MODE, int K, int C>
+struct Geo {
+  static constexpr int R = K / 2;
+  static constexpr int ES = ModeTraits<MODE>::ES;
+  static constexpr int HALO_ELEMS = MODE == MODE_BLURDOWN ? 2 * C + 2 : R * C;
+  static constexpr int HC = (HALO_ELEMS * ES + kChunk - 1) / kChunk;  // halo chunks / side
+  static constexpr int HW = 4 * HC;                                   // halo words / side
+  static constexpr int NW = 4 + 2 * HW;  // 32-bit words read around a chunk
+  static constexpr bool PACKED = ModeTraits<MODE>::LANES && K >= 15;
+};
+
+// ---------------------------------------------------------------------------
+// Border map (single fold; exact for n >= K - 1).  Positions that are farther
+// than one fold from the image are only ever read by halo lanes whose results
+// are discarded, so they are clamped to stay inside the allocation.
+__device__ __forceinline__ int map_index(int i, int n, int border) {
+  if (static_cast<unsigned>(i) < static_cast<unsigned>(n)) return i;
+  int m;
+  switch (border) {
+    case BORDER_REPLICATE: m = i < 0 ? 0 : n - 1; break;
+    case BORDER_REFLECT: m = i < 0 ? -i - 1 : 2 * n - i - 1; break;
+    case BORDER_WRAP: m = i < 0 ? i + n : i - n; break;
+    case BORDER_REVERSE: m = i < 0 ? -i : 2 * n - i - 2; break;
+    default: return -1;  // CONSTANT
+  }
+  return m < 0 ? 0 : (m >= n ? n - 1 : m);
+}
+
+// Loads the in-image 16 bytes of a row at byte offset xb (0 <= xb, xb + 16 <=
+// row bytes) with 16-byte loads: directly when aligned, otherwise from the two
+// aligned blocks covering it when both lie inside the row.  Returns false when
+// neither applies (the caller then assembles the chunk element by element).
+__device__ __forceinline__ bool load_chunk_fast(const uint8_t *row, long xb, long wcb, uint4 &out) {
+  const uint8_t *p = row + xb;
+  const uintptr_t pa = reinterpret_cast<uintptr_t>(p);
+  if ((pa & 15) == 0) {
+    out = ld_nc_v4(p);
+    return true;
+  }
+  const uint8_t *a = reinterpret_cast<const uint8_t *>(pa & ~static_cast<uintptr_t>(15));
+  if (a < row || a + 32 > row + wcb) return false;
+  const uint4 u = ld_nc_v4(a), v = ld_nc_v4(a + 16);
+  const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
+  const int sh = static_cast<int>(pa & 15), q = sh >> 2, s8 = (sh & 3) * 8;
+  uint32_t o[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t lo = q == 0 ? w[k] : q == 1 ? w[k + 1] : q == 2 ? w[k + 2] : w[k + 3];
+    const uint32_t hi = q == 0 ? w[k + 1] : q == 1 ? w[k + 2] : q == 2 ? w[k + 3] : w[k + 4];
+    o[k] = __funnelshift_r(lo, hi, s8);
+  }
+  out = make_uint4(o[0], o[1], o[2], o[3]);
+  return true;
+}
+
+// Where the bytes of one tile row live in a ring stage.
+struct SpanGeo {
+  long xs;        // first byte of the span (multiple of 16, may be negative)
+  long span_end;  // xs + boxes * box bytes
+  long wcb;       // bytes per image row
+  long wrapl_x;   // first byte of the left wrap area's box (valid if wrap_left)
+  int lbw;        // log2 of the span box width in bytes (256 or 2048)
+  int rb;         // rows per stage
+  int span_area;  // bytes of a stage taken by the span boxes
+  bool wrap_left, wrap_right;
+};
+
+// Offset within a stage of byte `o` of the span in row r ([box][row][box bytes]).
+__device__ __forceinline__ int span_offset(const SpanGeo &g, int r, int o) {
+  const int bw = 1 << g.lbw;
+  return (o >> g.lbw) * g.rb * bw + r * bw + (o & (bw - 1));
+}
+
+// Byte `b` (absolute offset within the image row) of stage row `r`, from the
+// span or a wrap area.  Bytes that were not staged read as 0; only halo lanes
+// whose results are discarded can ask for them.
+__device__ __forceinline__ uint32_t staged_byte(const uint8_t *slot, const SpanGeo &g, int r,
+                                                long b) {
+  if (b >= g.xs && b < g.span_end) return slot[span_offset(g, r, static_cast<int>(b - g.xs))];
+  const uint8_t *wrap = slot + g.span_area;
+  if (g.wrap_left && b >= g.wrapl_x && b < g.wrapl_x + 256) return wrap[r * 256 + (b - g.wrapl_x)];
+  if (g.wrap_right && b >= 0 && b < 256) return wrap[g.rb * 256 + r * 256 + b];
+  return 0;
+}
+
+// Source element index that border-maps to element x of a row (x outside the
+// row), or -1 for a CONSTANT border.
+template <int C>
+__device__ __forceinline__ long mapped_element(const FilterJob &j, long x) {
+  const long col = x >= 0 ? x / C : -((-x + C - 1) / C);
+  const int ch = static_cast<int>(x - col * C);
+  const int mc = map_index(static_cast<int>(col), j.width, j.border);
+  return mc < 0 ? -1 : static_cast<long>(mc) * C + ch;
+}
+
+// ---------------------------------------------------------------------------
+// Per-thread row representations.
+struct LaneRow {  // 16 u8 elements as 16-bit lanes: lo = elements 4i, 4i+2; hi = 4i+1, 4i+3
+  uint32_t lo[4], hi[4];
+};
+struct RawRow {  // 16 raw bytes (packed window for large kernels)
+  uint32_t w[4];
+};
+struct U32Row {  // 8 u16 elements widened to u32
+  uint32_t e[8];
+};
+struct S32Row {  // 8 s16 elements sign-extended
+  int32_t e[8];
+};
+
+template <int MODE, int K>
+struct RowOf {
+  using type = std::conditional_t<
+      MODE == MODE_SEP_U16, U32Row,
+      std::conditional_t<MODE == MODE_SEP_S16, S32Row,
+                         std::conditional_t<(K >= 15), RawRow, LaneRow>>>;
+};
+
+__device__ __forceinline__ uint32_t lanes_lo(uint32_t w) { return w & 0x00FF00FFu; }
+__device__ __forceinline__ uint32_t lanes_hi(uint32_t w) { return (w >> 8) & 0x00FF00FFu; }
+
+template <int MODE, int K>
+__device__ __forceinline__ void unpack_row(const uint4 &raw, typename RowOf<MODE, K>::type &r) {
+  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+  using Row = typename RowOf<MODE, K>::type;
+  if constexpr (std::is_same_v<Row, LaneRow>) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      r.lo[i] = lanes_lo(w[i]);
+      r.hi[i] = lanes_hi(w[i]);
+    }
+  } else if constexpr (std::is_same_v<Row, RawRow>) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.w[i] = w[i];
+  } else if constexpr (std::is_same_v<Row, U32Row>) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      r.e[2 * i] = w[i] & 0xFFFFu;
+      r.e[2 * i + 1] = w[i] >> 16;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      r.e[2 * i] = static_cast<int32_t>(static_cast<int16_t>(w[i] & 0xFFFFu));
+      r.e[2 * i + 1] = static_cast<int32_t>(w[i]) >> 16;
+    }
+  }
+}
+
+// Lane j (0..7 over lo[0..3], hi[0..3]) of a lane-form or packed row.
+template <int J>
+__device__ __forceinline__ uint32_t lane_reg(const LaneRow &r) {
+  return J < 4 ? r.lo[J & 3] : r.hi[J & 3];
+}
+template <int J>
+__device__ __forceinline__ uint32_t lane_reg(const RawRow &r) {
+  return J < 4 ? lanes_lo(r.w[J & 3]) : lanes_hi(r.w[J & 3]);
+}
+
+// Binomial coefficient sets and rounding shifts of the reference
+// (gaussian_blur_fixed_neon.cpp: 3x3 :27-85, 5x5 :87-153, 7x7 :155-281,
+// 9x9 :283-459).
+template <int K>
+struct Binomial;
+template <>
+struct Binomial<3> {
+  __host__ __device__ static constexpr int c(int i) { return i == 1 ? 2 : 1; }
+  static constexpr int shift = 4;
+};
+template <>
+struct Binomial<5> {
+  __host__ __device__ static constexpr int c(int i) {
+    return i == 2 ? 6 : (i == 1 || i == 3) ? 4 : 1;
+  }
+  static constexpr int shift = 8;
+};
+template <>
+struct Binomial<7> {
+  __host__ __device__ static constexpr int c(int i) {
+    return i == 3 ? 18 : (i == 2 || i == 4) ? 14 : (i == 1 || i == 5) ? 7 : 2;
+  }
+  static constexpr int shift = 12;
+};
+template <>
+struct Binomial<9> {
+  __host__ __device__ static constexpr int c(int i) {
+    return i == 4 ? 60 : (i == 3 || i == 5) ? 51 : (i == 2 || i == 6) ? 30
+           : (i == 1 || i == 7) ? 13 : 4;
+  }
+  static constexpr int shift = 16;
+};
+
+// Taps held in registers for the duration of a tile.
+struct Taps {
+  uint32_t y[kMaxTaps];
+  uint32_t x[kMaxTaps];
+};
+
+// ---------------------------------------------------------------------------
+// Vertical pass over the window.  Tap t lives in slot (ROT + t) % K.
+// Output: lane form (u8 modes), u32 (u16), s32 (s16).
+
+template <int MODE, int K, int ROT, typename Row>
+__device__ __forceinline__ void vertical_lanes(const Row (&win)[K], const Taps &tp,
+                                               uint32_t (&v)[8]) {
+  constexpr int R = K / 2;
+  static_for<0, 8>([&](auto jc) {
+    constexpr int J = decltype(jc)::value;
+    uint32_t acc;
+    if constexpr (MODE == MODE_SIGMA) {
+      // (sum + 128) >> 8 kept in 16-bit lanes: the weights sum to 256 so a lane
+      // never exceeds 255*256 + 128 (fixed sizes: gaussian_blur_fixed_neon.cpp:501-526).
+      acc = 0x00800080u + tp.y[R] * lane_reg<J>(win[(ROT + R) % K]);
+      static_for<0, R>([&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        acc += tp.y[I] * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
+      });
+      v[J] = (acc >> 8) & 0x00FF00FFu;
+    } else if constexpr (MODE == MODE_BINOM || MODE == MODE_BLURDOWN) {
+      using B = Binomial<(MODE == MODE_BLURDOWN ? 5 : K)>;
+      acc = B::c(R) * lane_reg<J>(win[(ROT + R) % K]);
+      static_for<0, R>([&](auto ic) {
+        constexpr int I = decltype(ic)::value;
+        acc += B::c(I) * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
+      });
+      v[J] = acc;  // exact, <= 255 * 256
+    } else {       // MODE_SEP_U8: saturating u16 in the reference; any lane that
+                   // reaches 255 forces a 255 output (taps are non-negative), so
+                   // clamping every product and the sum to 255 gives the same bytes.
+      acc = 0;
+      static_for<0, K>([&](auto tc) {
+        constexpr int T = decltype(tc)::value;
+        acc += vmin_u16x2(tp.y[T] * lane_reg<J>(win[(ROT + T) % K]), 0x00FF00FFu);
+      });
+      v[J] = vmin_u16x2(acc, 0x00FF00FFu);
+    }
+  });
+}
+
+template <int K, int ROT>
+__device__ __forceinline__ void vertical_u16(const U32Row (&win)[K], const Taps &tp,
+                                             uint32_t (&v)[8]) {
+  // separable_filter_2d_neon.cpp:140-158: saturating u32 sums of u16 x u16
+  // products, then a saturating narrow of the horizontal sum.  Clamping each
+  // product and the vertical sum to 65535 yields identical outputs because the
+  // taps are non-negative.
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    uint32_t acc = 0;
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      acc += min(tp.y[T] * win[(ROT + T) % K].e[e], 0xFFFFu);
+    });
+    v[e] = min(acc, 0xFFFFu);
+  }
+}
+
+template <int K, int ROT>
+__device__ __forceinline__ void vertical_s16(const S32Row (&win)[K], const Taps &tp,
+                                             int32_t (&v)[8]) {
+  // Extension semantics: tap-0 product, then saturating s32 adds in tap order.
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    int32_t acc = static_cast<int32_t>(tp.y[0]) * win[ROT % K].e[e];
+    static_for<1, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      acc = add_sat_s32(acc, static_cast<int32_t>(tp.y[T]) * win[(ROT + T) % K].e[e]);
+    });
+    v[e] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Horizontal pass helpers for the lane form.  lo/hi hold NW words around the
+// thread's own 4 words (which start at index HW).  Returns the pair of lanes
+// for elements (4*I + P + D, 4*I + P + D + 2) of the thread's span.
+template <int HW, int NW, int I, int P, int D>
+__device__ __forceinline__ uint32_t pair_at(const uint32_t (&lo)[NW], const uint32_t (&hi)[NW]) {
+  constexpr int g = P + D;
+  constexpr int q = floor_div(g, 4);
+  constexpr int rem = g - 4 * q;
+  constexpr int w = HW + I + q;
+  static_assert(w >= 0 && w + (rem >= 2 ? 1 : 0) < NW, "halo too small");
+  if constexpr ((rem & 1) == 0) {
+    if constexpr (rem < 2) return lo[w];
+    else return __byte_perm(lo[w], lo[w + 1], 0x5432);
+  } else {
+    if constexpr (rem < 2) return hi[w];
+    else return __byte_perm(hi[w], hi[w + 1], 0x5432);
+  }
+}
+
+// Computes the 16 output bytes of the thread for lane-form modes.
+template <int MODE, int K, int C>
+__device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const uint32_t *vhi_s,
+                                                  int tid, const Taps &tp) {
+  using G = Geo<MODE, K, C>;
+  constexpr int R = K / 2, HW = G::HW, NW = G::NW;
+  uint32_t lo[NW], hi[NW];
+  const int base = 4 * tid - HW;
+#pragma unroll
+  for (int k = 0; k < NW; k += 4) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(vlo_s + base + k);
+    const uint4 b = *reinterpret_cast<const uint4 *>(vhi_s + base + k);
+    lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
+    hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
+  }
+  uint32_t out[4];
+  static_for<0, 4>([&](auto ic) {
+    constexpr int I = decltype(ic)::value;
+    uint32_t res[2];
+    static_for<0, 2>([&](auto pc) {
+      constexpr int P = decltype(pc)::value;
+      if constexpr (MODE == MODE_SIGMA) {
+        // Gaussian kernels are identical in both directions: reuse tp.y.
+        uint32_t acc = 0x00800080u + tp.y[R] * pair_at<HW, NW, I, P, 0>(lo, hi);
+        static_for<1, R + 1>([&](auto dc) {
+          constexpr int D = decltype(dc)::value;
+          acc += tp.y[R - D] * (pair_at<HW, NW, I, P, -D * C>(lo, hi) +
+                                pair_at<HW, NW, I, P, D * C>(lo, hi));
+        });
+        res[P] = acc;
+      } else if constexpr (MODE == MODE_SEP_U8) {
+        uint32_t acc = 0;
+        static_for<0, K>([&](auto tc) {
+          constexpr int T = decltype(tc)::value;
+          acc += vmin_u16x2(tp.x[T] * pair_at<HW, NW, I, P, (T - R) * C>(lo, hi), 0x00FF00FFu);
+        });
+        res[P] = vmin_u16x2(acc, 0x00FF00FFu);
+      } else {  // MODE_BINOM
+        using B = Binomial<K>;
+        if constexpr (K <= 5) {
+          // Fits 16-bit lanes: 5x5 sums to 255*16*16, 3x3 to 255*4*4.
+          uint32_t acc = (1u << (B::shift - 1)) * 0x00010001u +
+                         B::c(R) * pair_at<HW, NW, I, P, 0>(lo, hi);
+          static_for<1, R + 1>([&](auto dc) {
+            constexpr int D = decltype(dc)::value;
+            acc += B::c(R - D) * (pair_at<HW, NW, I, P, -D * C>(lo, hi) +
+                                  pair_at<HW, NW, I, P, D * C>(lo, hi));
+          });
+          res[P] = acc;
+        } else {
+          // 7x7 / 9x9 need 32-bit sums (u32 in the reference, :220-279, :395-438).
+          uint32_t a0 = 1u << (B::shift - 1), a1 = a0;
+          static_for<0, K>([&](auto tc) {
+            constexpr int T = decltype(tc)::value;
+            const uint32_t pr = pair_at<HW, NW, I, P, (T - R) * C>(lo, hi);
+            a0 += B::c(T) * (pr & 0xFFFFu);
+            a1 += B::c(T) * (pr >> 16);
+          });
+          res[P] = ((a0 >> B::shift) & 0xFFu) | (((a1 >> B::shift) & 0xFFu) << 16);
+        }
+      }
+    });
+    // Pack lanes back to bytes: element order 4I, 4I+1, 4I+2, 4I+3.
+    if constexpr (MODE == MODE_SIGMA || (MODE == MODE_BINOM && K == 5)) {
+      out[I] = __byte_perm(res[0], res[1], 0x7351);  // high byte of each lane
+    } else if constexpr (MODE == MODE_BINOM && K == 3) {
+      out[I] = __byte_perm((res[0] >> 4) & 0x00FF00FFu, (res[1] >> 4) & 0x00FF00FFu, 0x6240);
+    } else {
+      out[I] = __byte_perm(res[0], res[1], 0x6240);  // low byte of each lane
+    }
+  });
+  return make_uint4(out[0], out[1], out[2], out[3]);
+}
+
+// u16 separable: V row is u16 elements (same layout as the input row).
+template <int K, int C>
+__device__ __forceinline__ uint4 horizontal_u16(const uint32_t *v_s, int tid, const Taps &tp) {
+  using G = Geo<MODE_SEP_U16, K, C>;
+  constexpr int R = K / 2, HW = G::HW, NW = G::NW;
+  uint32_t w[NW];
+  const int base = 4 * tid - HW;
+#pragma unroll
+  for (int k = 0; k < NW; k += 4) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(v_s + base + k);
+    w[k] = a.x; w[k + 1] = a.y; w[k + 2] = a.z; w[k + 3] = a.w;
+  }
+  uint32_t o[8];
+  static_for<0, 8>([&](auto ec) {
+    constexpr int E = decltype(ec)::value;
+    uint32_t acc = 0;
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      constexpr int el = 2 * HW + E + (T - R) * C;  // element index into w (2 per word)
+      static_assert(el >= 0 && el / 2 < NW, "halo too small");
+      const uint32_t val = (el & 1) ? (w[el / 2] >> 16) : (w[el / 2] & 0xFFFFu);
+      acc += min(tp.x[T] * val, 0xFFFFu);
+    });
+    o[E] = min(acc, 0xFFFFu);
+  });
+  return make_uint4(o[0] | (o[1] << 16), o[2] | (o[3] << 16), o[4] | (o[5] << 16),
+                    o[6] | (o[7] << 16));
+}
+
+// s16 separable: V row is s32 elements.
+template <int K, int C>
+__device__ __forceinline__ uint4 horizontal_s16(const int32_t *v_s, int tid, const Taps &tp) {
+  using G = Geo<MODE_SEP_S16, K, C>;
+  constexpr int R = K / 2, HE = 2 * G::HW, NE = 8 + 2 * HE;  // elements
+  int32_t v[NE];
+  const int base = 8 * tid - HE;
+#pragma unroll
+  for (int k = 0; k < NE; k += 4) {
+    const int4 a = *reinterpret_cast<const int4 *>(v_s + base + k);
+    v[k] = a.x; v[k + 1] = a.y; v[k + 2] = a.z; v[k + 3] = a.w;
+  }
+  uint32_t o[8];
+  static_for<0, 8>([&](auto ec) {
+    constexpr int E = decltype(ec)::value;
+    int64_t acc = 0;
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      constexpr int el = HE + E + (T - R) * C;
+      static_assert(el >= 0 && el < NE, "halo too small");
+      acc += static_cast<int64_t>(static_cast<int32_t>(tp.x[T])) * v[el];
+    });
+    const int64_t c = acc > 32767 ? 32767 : (acc < -32768 ? -32768 : acc);
+    o[E] = static_cast<uint32_t>(c) & 0xFFFFu;
+  });
+  return make_uint4(o[0] | (o[1] << 16), o[2] | (o[3] << 16), o[4] | (o[5] << 16),
+                    o[6] | (o[7] << 16));
+}
+
+// blur_and_downsample: the thread produces the 8 destination bytes whose
+// source centres lie in its chunk.  Destination element o (absolute) has
+// channel ch = o % C and source centre 2*o - ch; taps are centre + d*C with
+// the binomial [1 4 6 4 1] (blur_and_downsample_neon.cpp:128-177).
+template <int C>
+__device__ __forceinline__ uint2 horizontal_blurdown(const uint32_t *vlo_s, const uint32_t *vhi_s,
+                                                     int tid, long out_elem0, int span_elem0) {
+  uint32_t o[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const long oe = out_elem0 + k;
+    const int ch = static_cast<int>(oe % C);
+    const int centre = static_cast<int>(2 * oe - ch - span_elem0);  // index into the span
+    uint32_t acc = 128;
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const int e = centre + d * C;
+      const uint32_t *arr = (e & 1) ? vhi_s : vlo_s;
+      const uint32_t word = arr[e >> 2];
+      const uint32_t val = ((e >> 1) & 1) ? (word >> 16) : (word & 0xFFFFu);
+      const uint32_t c = (d == 0) ? 6u : ((d == 1 || d == -1) ? 4u : 1u);
+      acc += c * val;
+    }
+    o[k] = (acc >> 8) & 0xFFu;
+  }
+  (void)tid;
+  return make_uint2(o[0] | (o[1] << 8) | (o[2] << 16) | (o[3] << 24),
+                    o[4] | (o[5] << 8) | (o[6] << 16) | (o[7] << 24));
+}
+
+// ---------------------------------------------------------------------------
+// CTA organisation.  `warps` consumer warps each own 32 consecutive chunks
+// (16 bytes of a row per lane): an interior of 32 - 2*HC chunks plus HC halo
+// chunks on either side, which overlap the neighbouring warps' interiors.  A
+// warp therefore needs no other warp's data and synchronises only with
+// __syncwarp; the warps of a CTA share the TMA ring, fed by one extra
+// producer warp through full/empty mbarrier pairs.
+struct CtaShape {
+  int warps;        // consumer warps
+  int wi;           // interior chunks per warp
+  int span_chunks;  // chunks of a row the CTA reads: warps * wi + 2 * HC
+  int boxes;        // span boxes per row
+  int span_bytes;   // boxes * box width
+};
+
+__host__ __device__ inline CtaShape cta_shape(int threads, int hc, int lbw) {
+  CtaShape s;
+  const int bw = 1 << lbw;
+  s.warps = threads / 32 - 1;
+  s.wi = 32 - 2 * hc;
+  s.span_chunks = s.warps * s.wi + 2 * hc;
+  s.boxes = (s.span_chunks * kChunk + bw - 1) / bw;
+  s.span_bytes = s.boxes * bw;
+  return s;
+}
+
+template <int MODE>
+__host__ __device__ constexpr uint32_t vrow_bytes_per_lane() {
+  // lane form: lo + hi words (32 B); u16: 16 B; s32: 32 B.
+  return MODE == MODE_SEP_U16 ? 16u : 32u;
+}
+
+struct SmemLayout {
+  uint32_t ring_stage_bytes, span_area, v_off, v_warp_bytes, bar_off, total;
+};
+
+// A ring stage holds stage_rows rows.  With TMA: the staged span laid out as
+// [box][row][box bytes] followed by two 256-byte-wide wrap areas
+// ([area][row][256 B]) that receive the far end of the row when a WRAP border
+// needs it.  Without TMA every lane owns a private 16-byte slot per row
+// ([warp][row][32 x 16 B]).
+template <int MODE>
+__host__ __device__ inline SmemLayout smem_layout(int threads, int hc, int lbw, int stage_rows,
+                                                  int stages) {
+  const CtaShape s = cta_shape(threads, hc, lbw);
+  SmemLayout l;
+  const uint32_t tma_row = s.span_bytes + 512, own_row = s.warps * 32 * kChunk;
+  l.span_area = static_cast<uint32_t>(stage_rows) * s.span_bytes;
+  l.ring_stage_bytes = static_cast<uint32_t>(stage_rows) * (tma_row > own_row ? tma_row : own_row);
+  l.v_off = l.ring_stage_bytes * stages;
+  l.v_warp_bytes = 2 * 32 * vrow_bytes_per_lane<MODE>();  // double-buffered
+  l.bar_off = l.v_off + s.warps * l.v_warp_bytes;
+  l.total = l.bar_off + 16 * stages;  // full[stages] + empty[stages]
+  return l;
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s for any device-side wait
+
+// The tensor maps of one job.  Span maps view the row in units of 1 << (lbw-8)
+// bytes (1 or 8) so that one box is 256 such units wide; wrap maps always use
+// bytes.
+struct TmaMaps {
+  const CUtensorMap *span, *span_row, *wrap, *wrap_row;
+};
+
+// ---------------------------------------------------------------------------
+// One tile: strip `strip` x band `band` of job `j`.  `gstage` counts ring
+// stages used by this CTA so far (mbarrier phases continue across tiles).
+// stage_rows and stages are powers of two.
+template <int MODE, int K, int C>
+__device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps, int strip,
+                                         int band, uint8_t *smem, uint32_t &gstage,
+                                         int *err_flag, bool &timed_out) {
+  using G = Geo<MODE, K, C>;
+  using Row = typename RowOf<MODE, K>::type;
+  constexpr int ES = G::ES;
+  constexpr int HC = G::HC;
+  constexpr int E = kChunk / ES;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lbw = j.box_lbw;
+  const CtaShape sh = cta_shape(blockDim.x, HC, lbw);
+  const int rb = j.stage_rows, ns = j.stages;
+  const int lrb = __ffs(rb) - 1, lns = __ffs(ns) - 1;
+  const SmemLayout L = smem_layout<MODE>(blockDim.x, HC, lbw, rb, ns);
+  uint8_t *ring = smem;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+  uint64_t *empty = full + ns;
+
+  const int oy0 = band * j.tile_rows;
+  const int orows = min(j.tile_rows, j.out_height - oy0);
+  const int iy0 = MODE == MODE_BLURDOWN ? 2 * oy0 - 2 : oy0 - G::R;
+  const int in_rows = MODE == MODE_BLURDOWN ? 2 * orows + 3 : orows + K - 1;
+  const long xs = static_cast<long>(strip) * sh.warps * sh.wi * kChunk - HC * kChunk;
+  const long wc = static_cast<long>(j.width) * C;
+  const long wcb = wc * ES;
+  const bool use_tma = j.use_tma != 0;
+  const int nstages = (in_rows + rb - 1) >> lrb;
+
+  SpanGeo sg;
+  sg.xs = xs;
+  sg.span_end = xs + sh.span_bytes;
+  sg.wcb = wcb;
+  sg.lbw = lbw;
+  sg.rb = rb;
+  sg.span_area = static_cast<int>(L.span_area);
+  {
+    // The wrap areas are filled only for a WRAP border on a strip that touches
+    // exactly one side of the image (a strip spanning both sides already
+    // holds the far end of the row).
+    const bool left = xs < 0, right = sg.span_end > wcb;
+    sg.wrap_left = j.border == BORDER_WRAP && left && !right;
+    sg.wrap_right = j.border == BORDER_WRAP && right && !left;
+    const long hb = static_cast<long>(G::HALO_ELEMS) * ES;
+    sg.wrapl_x = wcb - hb > 0 ? ((wcb - hb) & ~15L) : 0;
+  }
+
+  // ======================= producer warp =======================
+  if (warp == sh.warps) {
+    if (use_tma && lane == 0) {
+      const int bw = 1 << lbw, unit_shift = lbw - 8;  // span map unit = 1 << unit_shift bytes
+      // fn(map, x in map units, destination, row-box) for every box of a stage.
+      auto for_each_box = [&](uint8_t *base, bool single_row, auto &&fn) {
+        for (int b = 0; b < sh.boxes; ++b) {
+          const long x = xs + static_cast<long>(b) * bw;
+          if (x < wcb && x + bw > 0)
+            fn(single_row ? maps.span_row : maps.span, x >> unit_shift, base + b * rb * bw,
+               static_cast<uint32_t>(bw));
+        }
+        uint8_t *wrap = base + L.span_area;
+        if (sg.wrap_left) fn(single_row ? maps.wrap_row : maps.wrap, sg.wrapl_x, wrap, 256u);
+        if (sg.wrap_right) fn(single_row ? maps.wrap_row : maps.wrap, 0L, wrap + rb * 256, 256u);
+      };
+      for (int s = 0; s < nstages && !timed_out; ++s) {
+        const uint32_t g = gstage + s;
+        const int slot = static_cast<int>(g & (ns - 1));
+        const uint32_t use = g >> lns;
+        if (use > 0 && !mbar_wait_bounded(&empty[slot], (use - 1) & 1u, kWaitLimitNs)) {
+          timed_out = true;
+          atomicOr(err_flag, 1);
+          break;
+        }
+        uint8_t *base = ring + slot * L.ring_stage_bytes;
+        uint64_t *bar = &full[slot];
+        // Rows inside the image arrive as stage_rows-high boxes; a stage that
+        // reaches outside gets one single-row box per row of its border-mapped
+        // source row instead (none for a CONSTANT border).
+        const int y = iy0 + s * rb;
+        const bool rows_in = y >= 0 && y + rb <= j.height;
+        uint32_t tx = 0;
+        if (rows_in) {
+          for_each_box(base, false, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) {
+            tx += w * rb;
+          });
+        } else {
+          for (int r = 0; r < rb; ++r)
+            if (map_index(y + r, j.height, j.border) >= 0)
+              for_each_box(base, true, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) {
+                tx += w;
+              });
+        }
+        if (tx == 0) {
+          mbar_arrive(bar);
+          continue;
+        }
+        mbar_arrive_expect_tx(bar, tx);
+        if (rows_in) {
+          for_each_box(base, false, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
+            tma_load_2d(d, m, static_cast<int>(x), y, bar);
+          });
+        } else {
+          for (int r = 0; r < rb; ++r) {
+            const int my = map_index(y + r, j.height, j.border);
+            if (my >= 0)
+              for_each_box(base, true, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t w) {
+                tma_load_2d(d + r * w, m, static_cast<int>(x), my, bar);
+              });
+          }
+        }
+      }
+      if (timed_out) {
+        // Give copies already issued a bounded time to land before the CTA's
+        // shared memory can be reused.
+        for (int s = 0; s < nstages; ++s) {
+          const uint32_t g = gstage + s;
+          mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs);
+        }
+      }
+    }
+    gstage += nstages;
+    return;
+  }
+
+  // ======================= consumer warps =======================
+  const int cidx = warp * sh.wi + lane;  // chunk index within the CTA span
+  const long xb = xs + static_cast<long>(cidx) * kChunk;
+  const bool chunk_in = xb >= 0 && xb + kChunk <= wcb;
+  // Chunks that start past the right halo only feed discarded lanes.
+  const bool active = xb < wcb + HC * kChunk;
+  const bool emits = lane >= HC && lane < 32 - HC;
+  // Destination rows all start 16-byte aligned when base and stride are.
+  const bool dst_rows_aligned =
+      ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 15) == 0;
+  // This lane writes a whole 16-byte chunk with one vector store.
+  const bool full_store = dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
+  const bool stores = emits && active && xb < wcb;
+  const uint32_t bv_elem = ES == 1 ? (static_cast<uint32_t>(j.border_value) & 0xFFu)
+                                   : (static_cast<uint32_t>(j.border_value) & 0xFFFFu);
+  const uint32_t bv_word = ES == 1 ? bv_elem * 0x01010101u : bv_elem * 0x00010001u;
+  // Where lane `l` of this warp keeps its chunk of row 0 of a stage, and the
+  // distance between rows.
+  auto chunk_offset = [&](int l) {
+    return use_tma ? span_offset(sg, 0, (warp * sh.wi + l) * kChunk) : (warp * rb * 32 + l) * kChunk;
+  };
+  const int row_pitch = use_tma ? (1 << lbw) : 32 * kChunk;
+  const int chunk_off = chunk_offset(lane);
+  // Lanes whose chunk is not plain image data in every row: hanging over the
+  // left/right edge, or (without TMA) not loadable with 16-byte loads.
+  // (load_chunk_fast succeeds in every row when the chunk is 16-byte aligned
+  // in every row, or when the two aligned blocks around it stay in the row
+  // whatever the row's misalignment.)
+  bool self_load_ok = chunk_in;
+  if (!use_tma && chunk_in) {
+    const uintptr_t pa = reinterpret_cast<uintptr_t>(j.src) + static_cast<uintptr_t>(xb);
+    self_load_ok = ((pa | static_cast<uintptr_t>(j.src_stride)) & 15) == 0 ||
+                   (xb >= 16 && xb + 32 <= wcb);
+  }
+  const unsigned coop_lanes = __ballot_sync(0xffffffffu, active && !self_load_ok);
+
+  Taps tp;
+  if constexpr (MODE == MODE_SIGMA) {
+#pragma unroll
+    for (int t = 0; t <= K / 2; ++t) tp.y[t] = static_cast<uint32_t>(j.wy[t]);
+  } else if constexpr (MODE != MODE_BINOM && MODE != MODE_BLURDOWN) {
+#pragma unroll
+    for (int t = 0; t < K; ++t) {
+      tp.y[t] = static_cast<uint32_t>(j.wy[t]);
+      tp.x[t] = static_cast<uint32_t>(j.wx[t]);
+    }
+  }
+
+  // Readies stage s for this warp.  With TMA: waits for the copies.  Without:
+  // every lane loads its own chunk of each row.  Then the warp jointly fills
+  // the chunks in `coop_lanes` one element per lane (border-mapped elements
+  // from the staged row, or from global memory without TMA), and every lane
+  // fills its chunk in rows lying in a CONSTANT border.  Lanes that share a
+  // chunk with a neighbouring warp write identical bytes.
+  auto prepare_stage = [&](int s) {
+    const uint32_t g = gstage + s;
+    uint8_t *base = ring + static_cast<int>(g & (ns - 1)) * L.ring_stage_bytes;
+    if (use_tma) {
+      if (!timed_out && !mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs)) {
+        timed_out = true;
+        atomicOr(err_flag, 1);
+      }
+    }
+    bool wrote = false;
+#pragma unroll 1
+    for (int r = 0; r < rb; ++r) {
+      const int q = s * rb + r;
+      const int iy = iy0 + q;
+      if (q >= in_rows) break;
+      if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) {
+        if (active) *reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch) =
+            make_uint4(bv_word, bv_word, bv_word, bv_word);
+        wrote = true;
+        continue;
+      }
+      const int ry = map_index(iy, j.height, j.border);
+      const uint8_t *grow = j.src + static_cast<int64_t>(ry) * j.src_stride;
+      if (!use_tma && active && self_load_ok) {
+        uint4 v;
+        load_chunk_fast(grow, xb, wcb, v);
+        *reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch) = v;
+      }
+      unsigned m = coop_lanes;
+      while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        const long xl = (xs + static_cast<long>(warp * sh.wi + l) * kChunk) / ES + lane;
+        if (lane < E) {
+          const bool inside = xl >= 0 && xl < wc;
+          if (!use_tma || !inside) {
+            const long me = inside ? xl : mapped_element<C>(j, xl);
+            uint32_t v;
+            if (me < 0) {
+              v = bv_elem;
+            } else if (use_tma) {
+              v = staged_byte(base, sg, r, me * ES);
+              if (ES == 2) v |= staged_byte(base, sg, r, me * ES + 1) << 8;
+            } else if (ES == 1) {
+              v = __ldg(grow + me);
+            } else {
+              v = __ldg(reinterpret_cast<const uint16_t *>(grow) + me);
+            }
+            uint8_t *dst = base + chunk_offset(l) + r * row_pitch + lane * ES;
+            dst[0] = static_cast<uint8_t>(v);
+            if (ES == 2) dst[1] = static_cast<uint8_t>(v >> 8);
+            wrote = true;
+          }
+        }
+      }
+    }
+    // Order these generic-proxy writes before any later TMA write to the slot.
+    if (use_tma && wrote) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncwarp();
+  };
+  // Hands stage s back to the producer once every lane of the warp has read it.
+  auto release_stage = [&](int s) {
+    if (!use_tma) return;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[(gstage + s) & (ns - 1)]);
+  };
+
+  uint32_t *vwarp = reinterpret_cast<uint32_t *>(smem + L.v_off + warp * L.v_warp_bytes);
+  constexpr uint32_t kVRowWords = 32 * vrow_bytes_per_lane<MODE>() / 4;
+  Row win[K];
+  int emitted = 0;
+  int stage_of_block = 0;  // stage of row qb
+  int row_of_block = 0;    // qb % rb
+
+  auto load_row = [&](int u, Row &dst_row) {
+    // Row qb + u: stage and row within it from the block's base, no division.
+    const int r = row_of_block + u;
+    const int s = stage_of_block + (r >> lrb);
+    const uint8_t *base = ring + static_cast<int>((gstage + s) & (ns - 1)) * L.ring_stage_bytes;
+    const uint4 raw =
+        *reinterpret_cast<const uint4 *>(base + chunk_off + (r & (rb - 1)) * row_pitch);
+    unpack_row<MODE, K>(raw, dst_row);
+  };
+
+  auto emit = [&](auto rot_c, int q) {
+    constexpr int ROT = decltype(rot_c)::value;
+    uint32_t *vbuf = vwarp + (emitted & 1) * kVRowWords;
+    // ---- vertical pass -> the warp's shared row
+    if (active) {
+      if constexpr (ModeTraits<MODE>::LANES) {
+        uint32_t v[8];
+        vertical_lanes<MODE, K, ROT>(win, tp, v);
+        *reinterpret_cast<uint4 *>(vbuf + 4 * lane) = make_uint4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<uint4 *>(vbuf + 128 + 4 * lane) = make_uint4(v[4], v[5], v[6], v[7]);
+      } else if constexpr (MODE == MODE_SEP_U16) {
+        uint32_t v[8];
+        vertical_u16<K, ROT>(win, tp, v);
+        *reinterpret_cast<uint4 *>(vbuf + 4 * lane) =
+            make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16),
+                       v[6] | (v[7] << 16));
+      } else {
+        int32_t v[8];
+        vertical_s16<K, ROT>(win, tp, v);
+        int32_t *vs = reinterpret_cast<int32_t *>(vbuf);
+        *reinterpret_cast<int4 *>(vs + 8 * lane) = make_int4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<int4 *>(vs + 8 * lane + 4) = make_int4(v[4], v[5], v[6], v[7]);
+      }
+    }
+    __syncwarp();
+    // ---- horizontal pass + store
+    if (emits && active) {
+      const int oy = MODE == MODE_BLURDOWN ? oy0 + (q - 4) / 2 : oy0 + q - (K - 1);
+      uint8_t *drow = j.dst + static_cast<int64_t>(oy) * j.dst_stride;
+      if constexpr (MODE == MODE_BLURDOWN) {
+        const long ob = xb / 2;  // destination byte (= element) offset
+        const long owc = static_cast<long>(j.out_width) * C;
+        if (ob < owc) {
+          const uint2 r = horizontal_blurdown<C>(vbuf, vbuf + 128, lane, ob,
+                                                 static_cast<int>(xb - lane * kChunk));
+          if (ob + 8 <= owc && (reinterpret_cast<uintptr_t>(drow + ob) & 7) == 0) {
+            *reinterpret_cast<uint2 *>(drow + ob) = r;
+          } else {
+            const uint32_t w2[2] = {r.x, r.y};
+            for (int k = 0; k < 8 && ob + k < owc; ++k)
+              drow[ob + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
+          }
+        }
+      } else if (stores) {
+        uint4 r;
+        if constexpr (ModeTraits<MODE>::LANES)
+          r = horizontal_lanes<MODE, K, C>(vbuf, vbuf + 128, lane, tp);
+        else if constexpr (MODE == MODE_SEP_U16)
+          r = horizontal_u16<K, C>(vbuf, lane, tp);
+        else
+          r = horizontal_s16<K, C>(reinterpret_cast<const int32_t *>(vbuf), lane, tp);
+        if (full_store) {
+          st_v4(drow + xb, r);
+        } else {
+          const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
+          for (int k = 0; k < kChunk && xb + k < wcb; ++k)
+            drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
+        }
+      }
+    }
+    ++emitted;
+  };
+
+  // ---- rows in blocks of K (window slot of every tap = compile-time index).
+  // Before a block, the stages of rows already consumed are released FIRST,
+  // then the stages the block's rows touch are readied (single call sites keep
+  // the rarely used border code out of the unrolled body).  A warp at block qb
+  // waits for stage (qb+K-1)/stage_rows, whose slot was last used by stage
+  // (qb+K-1)/stage_rows - stages; with stages >= (K-1)/stage_rows + 2 every
+  // warp has already released that stage, so the producer can always issue
+  // what the most advanced warp waits for, and a slower warp never waits for
+  // a faster one.
+  int ready = 0, released = 0;
+  for (int qb = 0; qb < in_rows; qb += K) {
+    const int last_stage = (min(qb + K, in_rows) - 1) >> lrb;
+    for (; released < ready && ((released + 1) << lrb) <= qb; ++released) release_stage(released);
+    for (; ready <= last_stage; ++ready) prepare_stage(ready);
+    stage_of_block = qb >> lrb;
+    row_of_block = qb & (rb - 1);
+    static_for<0, K>([&](auto uc) {
+      constexpr int U = decltype(uc)::value;
+      const int q = qb + U;
+      if (q < in_rows) {
+        load_row(U, win[U]);
+        bool do_emit;
+        if constexpr (MODE == MODE_BLURDOWN)
+          do_emit = q >= 4 && ((q - 4) & 1) == 0;
+        else
+          do_emit = q >= K - 1;
+        if (do_emit) emit(std::integral_constant<int, (U + 1) % K>{}, q);
+      }
+    });
+  }
+  for (; released < nstages; ++released) release_stage(released);
+  gstage += nstages;
+}
+
+// ---------------------------------------------------------------------------
+// Single-image launch: grid (strips, bands), threads = 32 * (warps + 1).
+template <int MODE, int K, int C>
+__global__ void __launch_bounds__(288, 1) sepfused_kernel(const __grid_constant__ FilterJob job,
+                                                          int *err_flag) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  constexpr int HC = Geo<MODE, K, C>::HC;
+  const SmemLayout L = smem_layout<MODE>(blockDim.x, HC, job.box_lbw, job.stage_rows, job.stages);
+  if (job.use_tma) {
+    if (threadIdx.x == 0) {
+      prefetch_tensormap(&job.tmap);
+      prefetch_tensormap(&job.tmap_row);
+      uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+      const int consumers = blockDim.x / 32 - 1;
+      for (int s = 0; s < job.stages; ++s) {
+        mbar_init(&full[s], 1);
+        mbar_init(&full[job.stages + s], consumers);
+      }
+      fence_mbar_init();
+    }
+    __syncthreads();
+  }
+  uint32_t gstage = 0;
+  bool timed_out = false;
+  const TmaMaps maps{&job.tmap, &job.tmap_row, &job.tmap_wrap, &job.tmap_wrap_row};
+  run_tile<MODE, K, C>(job, maps, blockIdx.x, blockIdx.y, smem, gstage, err_flag, timed_out);
+}
+
+}  // namespace kcv
