@@ -258,21 +258,18 @@ TileShape tile_shape_for(const FilterJob &j, int sm_count) {
     return t;
   const int hc = halo_chunks(j);
   const long chunks = (wcb + kChunk - 1) / kChunk;  // 16-byte chunks per source row
-  const int wi = 32 - 2 * hc;                        // interior chunks per consumer warp
-  int warps = static_cast<int>(std::min<long>(4, std::max<long>(1, (chunks + wi - 1) / wi)));
-  t.threads = 32 * (warps + 1);
+  const int wi = 32 - 2 * hc;                        // interior chunks per warp
+  const int warps = static_cast<int>(std::min<long>(4, std::max<long>(1, (chunks + wi - 1) / wi)));
+  t.threads = 32 * warps;
   const long strip_chunks = static_cast<long>(warps) * wi;
   const long strips = j.mode == MODE_BLURDOWN
                           ? (static_cast<long>(j.out_width) * j.channels + strip_chunks * 8 - 1) /
                                 (strip_chunks * 8)
                           : (chunks + strip_chunks - 1) / strip_chunks;
-  const long target = 3L * std::max(sm_count, 1);
-  long bands = std::max(1L, target / std::max(strips, 1L));
-  int rows = static_cast<int>((j.out_height + bands - 1) / bands);
-  rows = std::max(8, std::min(rows, 512));
-  t.tile_rows = rows;
+  (void)strips;
+  t.tile_rows = 0;  // chosen from the measured occupancy (finish_plan)
   t.stage_rows = 4;
-  t.stages = 8;
+  t.stages = 4;
   return t;
 }
 
@@ -301,11 +298,8 @@ void apply_tile_shape(FilterJob &j, const TileShape &t) {
   j.stages = t.stages;
   fix_ring(j);
   j.halo_chunks = halo_chunks(j);
-  // Consumer warps x interior chunks per warp (one producer warp on top).
-  const int interior = (j.threads / 32 - 1) * (32 - 2 * j.halo_chunks);
-  // Row bands: gridDim.y is limited to 65535.
-  if ((j.out_height + j.tile_rows - 1) / j.tile_rows > 65535)
-    j.tile_rows = (j.out_height + 65534) / 65535;
+  // Warps x interior chunks per warp.
+  const int interior = (j.threads / 32) * (32 - 2 * j.halo_chunks);
   if (j.mode == MODE_BLURDOWN) {
     j.strip_out_bytes = interior * 8;
     j.strips = static_cast<int32_t>(
@@ -313,6 +307,19 @@ void apply_tile_shape(FilterJob &j, const TileShape &t) {
   } else {
     j.strip_out_bytes = interior * kChunk;
     j.strips = static_cast<int32_t>((wcb + j.strip_out_bytes - 1) / j.strip_out_bytes);
+  }
+  j.row_tiles = j.tile_rows > 0 ? (j.out_height + j.tile_rows - 1) / j.tile_rows : 0;
+}
+
+// Tile rows when the tile shape left them open: one tile per resident CTA of
+// a single wave (persistent CTAs walk the tiles), at least 8 rows per tile.
+void finish_plan(FilterJob &j, int sm_count) {
+  if (j.tile_rows <= 0) {
+    const int occ = std::max(1, fused_blocks_per_sm(j));
+    const long target = static_cast<long>(occ) * std::max(sm_count, 1);
+    const long bands = std::max(1L, target / std::max<long>(j.strips, 1));
+    int rows = static_cast<int>((j.out_height + bands - 1) / bands);
+    j.tile_rows = std::max(8, std::min(rows, 1 << 20));
   }
   j.row_tiles = (j.out_height + j.tile_rows - 1) / j.tile_rows;
 }
@@ -403,6 +410,7 @@ kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
     case Prepared::FUSED: {
       plan_fused(p.fused, ctx->sm_count);
       encode_tma(p.fused);
+      finish_plan(p.fused, ctx->sm_count);
       cudaError_t e = launch_fused(p.fused, ctx->d_err, ctx->stream);
       ctx->launches += 1;
       return cuda_status(ctx, e);

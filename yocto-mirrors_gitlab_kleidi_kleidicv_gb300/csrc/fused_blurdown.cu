@@ -1,8 +1,8 @@
 #include "fused_inst.cuh"
 namespace kcv {
-bool launch_fused_blurdown(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out) {
+bool launch_fused_blurdown(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out, int *o) {
   if (j.mode != MODE_BLURDOWN) return false;
-  return dispatch_channels<MODE_BLURDOWN, 5>(j, e, s, out);
+  return dispatch_channels<MODE_BLURDOWN, 5>(j, e, s, out, o);
 }
 size_t fused_smem_bytes(const FilterJob &job) {
   switch (job.mode) {
@@ -10,13 +10,23 @@ size_t fused_smem_bytes(const FilterJob &job) {
     default: return smem_layout<MODE_SIGMA>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages).total;
   }
 }
+static bool dispatch_fused(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
+                           int *occ) {
+  return launch_fused_binom(job, err, s, out, occ) ||
+         launch_fused_sigma_small(job, err, s, out, occ) ||
+         launch_fused_sigma_9(job, err, s, out, occ) ||
+         launch_fused_sigma_15(job, err, s, out, occ) ||
+         launch_fused_sigma_21(job, err, s, out, occ) || launch_fused_sep(job, err, s, out, occ) ||
+         launch_fused_blurdown(job, err, s, out, occ);
+}
 cudaError_t launch_fused(const FilterJob &job, int *err, cudaStream_t s) {
   cudaError_t out = cudaErrorInvalidValue;
-  if (launch_fused_binom(job, err, s, &out) || launch_fused_sigma_small(job, err, s, &out) ||
-      launch_fused_sigma_9(job, err, s, &out) || launch_fused_sigma_15(job, err, s, &out) ||
-      launch_fused_sigma_21(job, err, s, &out) || launch_fused_sep(job, err, s, &out) ||
-      launch_fused_blurdown(job, err, s, &out))
-    return out;
-  return cudaErrorInvalidValue;
+  return dispatch_fused(job, err, s, &out, nullptr) ? out : cudaErrorInvalidValue;
+}
+int fused_blocks_per_sm(const FilterJob &job) {
+  cudaError_t out = cudaErrorInvalidValue;
+  int occ = 0;
+  if (!dispatch_fused(job, nullptr, nullptr, &out, &occ) || out != cudaSuccess) return 0;
+  return occ;
 }
 }  // namespace kcv

@@ -1,14 +1,19 @@
 // Helpers shared by the fused-kernel instantiation units.
 #pragma once
 
+#include <algorithm>
+
 #include "launch.h"
 #include "sepfused.cuh"
 
 namespace kcv {
 
+// err_flag == nullptr: only report the occupancy in *blocks_per_sm.
 template <int MODE, int K, int C>
-cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream) {
-  const SmemLayout L = smem_layout<MODE>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages);
+cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
+                       int *blocks_per_sm = nullptr) {
+  const SmemLayout L =
+      smem_layout<MODE>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages);
   auto kern = sepfused_kernel<MODE, K, C>;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
@@ -17,17 +22,30 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream)
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  kern<<<dim3(job.strips, job.row_tiles), job.threads, L.total, stream>>>(job, err_flag);
+  // One wave of persistent CTAs: as many as fit on the device at once.
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, job.threads, L.total);
+  if (e != cudaSuccess) return e;
+  if (blocks_per_sm) {
+    *blocks_per_sm = per_sm;
+    return cudaSuccess;
+  }
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long tiles = static_cast<long>(job.strips) * job.row_tiles;
+  const long grid = std::max(1L, std::min(tiles, static_cast<long>(std::max(per_sm, 1)) * sms));
+  kern<<<static_cast<unsigned>(grid), job.threads, L.total, stream>>>(job, err_flag);
   return cudaGetLastError();
 }
 
 template <int MODE, int K>
-bool dispatch_channels(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out) {
+bool dispatch_channels(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
+                       int *blocks_per_sm = nullptr) {
   switch (job.channels) {
-    case 1: *out = launch_one<MODE, K, 1>(job, err, s); return true;
-    case 2: *out = launch_one<MODE, K, 2>(job, err, s); return true;
-    case 3: *out = launch_one<MODE, K, 3>(job, err, s); return true;
-    case 4: *out = launch_one<MODE, K, 4>(job, err, s); return true;
+    case 1: *out = launch_one<MODE, K, 1>(job, err, s, blocks_per_sm); return true;
+    case 2: *out = launch_one<MODE, K, 2>(job, err, s, blocks_per_sm); return true;
+    case 3: *out = launch_one<MODE, K, 3>(job, err, s, blocks_per_sm); return true;
+    case 4: *out = launch_one<MODE, K, 4>(job, err, s, blocks_per_sm); return true;
   }
   return false;
 }

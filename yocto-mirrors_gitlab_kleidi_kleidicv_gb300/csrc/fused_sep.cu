@@ -1,11 +1,11 @@
 #include "fused_inst.cuh"
 namespace kcv {
-bool launch_fused_sep(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out) {
+bool launch_fused_sep(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out, int *o) {
   if (j.ksize != 5) return false;
   switch (j.mode) {
-    case MODE_SEP_U8: return dispatch_channels<MODE_SEP_U8, 5>(j, e, s, out);
-    case MODE_SEP_U16: return dispatch_channels<MODE_SEP_U16, 5>(j, e, s, out);
-    case MODE_SEP_S16: return dispatch_channels<MODE_SEP_S16, 5>(j, e, s, out);
+    case MODE_SEP_U8: return dispatch_channels<MODE_SEP_U8, 5>(j, e, s, out, o);
+    case MODE_SEP_U16: return dispatch_channels<MODE_SEP_U16, 5>(j, e, s, out, o);
+    case MODE_SEP_S16: return dispatch_channels<MODE_SEP_S16, 5>(j, e, s, out, o);
   }
   return false;
 }

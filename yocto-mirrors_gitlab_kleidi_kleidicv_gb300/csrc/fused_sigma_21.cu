@@ -1,7 +1,7 @@
 #include "fused_inst.cuh"
 namespace kcv {
-bool launch_fused_sigma_21(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out) {
+bool launch_fused_sigma_21(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out, int *o) {
   if (j.mode != MODE_SIGMA || j.ksize != 21) return false;
-  return dispatch_channels<MODE_SIGMA, 21>(j, e, s, out);
+  return dispatch_channels<MODE_SIGMA, 21>(j, e, s, out, o);
 }
 }  // namespace kcv

@@ -67,6 +67,8 @@ kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t 
 // Chooses the tile shape (autotune table, else heuristic) and fills the
 // derived tiling fields of a FUSED job.  sm_count sizes the grid.
 void plan_fused(FilterJob &j, int sm_count);
+// Picks tile rows from the kernel's occupancy (after encode_tma).
+void finish_plan(FilterJob &j, int sm_count);
 TileShape tile_shape_for(const FilterJob &j, int sm_count);
 void apply_tile_shape(FilterJob &j, const TileShape &t);
 // Builds the TMA descriptor when the source allows it; sets j.use_tma.

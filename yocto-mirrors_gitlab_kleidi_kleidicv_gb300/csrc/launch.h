@@ -15,15 +15,20 @@ size_t fused_smem_bytes(const FilterJob &job);
 // instantiation exists for the combination.
 cudaError_t launch_fused(const FilterJob &job, int *err_flag, cudaStream_t stream);
 
+// Resident CTAs per SM of the fused kernel for `job`'s block size and shared
+// memory (0 if no instantiation exists).
+int fused_blocks_per_sm(const FilterJob &job);
+
 // Per-family dispatchers (one translation unit each); return false if the
-// (mode, ksize, channels) combination is not theirs.
-bool launch_fused_binom(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_sigma_small(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_sigma_9(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_sigma_15(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_sigma_21(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *);
-bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *);
+// (mode, ksize, channels) combination is not theirs.  With blocks_per_sm set
+// they only report the occupancy instead of launching.
+bool launch_fused_binom(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_sigma_small(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_sigma_9(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_sigma_15(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_sigma_21(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
 
 // Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
 // generated kernel whose weights do not sum to 256).  `scratch` holds the

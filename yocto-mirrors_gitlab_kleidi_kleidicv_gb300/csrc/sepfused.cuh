@@ -143,16 +143,6 @@ __device__ __forceinline__ uint32_t staged_byte(const uint8_t *slot, const SpanG
   return 0;
 }
 
-// Source element index that border-maps to element x of a row (x outside the
-// row), or -1 for a CONSTANT border.
-template <int C>
-__device__ __forceinline__ long mapped_element(const FilterJob &j, long x) {
-  const long col = x >= 0 ? x / C : -((-x + C - 1) / C);
-  const int ch = static_cast<int>(x - col * C);
-  const int mc = map_index(static_cast<int>(col), j.width, j.border);
-  return mc < 0 ? -1 : static_cast<long>(mc) * C + ch;
-}
-
 // ---------------------------------------------------------------------------
 // Per-thread row representations.
 struct LaneRow {  // 16 u8 elements as 16-bit lanes: lo = elements 4i, 4i+2; hi = 4i+1, 4i+3
@@ -177,7 +167,7 @@ struct RowOf {
 };
 
 __device__ __forceinline__ uint32_t lanes_lo(uint32_t w) { return w & 0x00FF00FFu; }
-__device__ __forceinline__ uint32_t lanes_hi(uint32_t w) { return (w >> 8) & 0x00FF00FFu; }
+__device__ __forceinline__ uint32_t lanes_hi(uint32_t w) { return __byte_perm(w, 0u, 0x4341); }
 
 template <int MODE, int K>
 __device__ __forceinline__ void unpack_row(const uint4 &raw, typename RowOf<MODE, K>::type &r) {
@@ -264,37 +254,59 @@ template <int MODE, int K, int ROT, typename Row>
 __device__ __forceinline__ void vertical_lanes(const Row (&win)[K], const Taps &tp,
                                                uint32_t (&v)[8]) {
   constexpr int R = K / 2;
-  static_for<0, 8>([&](auto jc) {
-    constexpr int J = decltype(jc)::value;
-    uint32_t acc;
-    if constexpr (MODE == MODE_SIGMA) {
-      // (sum + 128) >> 8 kept in 16-bit lanes: the weights sum to 256 so a lane
-      // never exceeds 255*256 + 128 (fixed sizes: gaussian_blur_fixed_neon.cpp:501-526).
-      acc = 0x00800080u + tp.y[R] * lane_reg<J>(win[(ROT + R) % K]);
-      static_for<0, R>([&](auto ic) {
-        constexpr int I = decltype(ic)::value;
-        acc += tp.y[I] * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
+  // Taps outer, lane registers inner: eight independent accumulation chains.
+  uint32_t acc[8];
+  if constexpr (MODE == MODE_SIGMA) {
+    // (sum + 128) >> 8 kept in 16-bit lanes: the weights sum to 256 so a lane
+    // never exceeds 255*256 + 128 (fixed sizes: gaussian_blur_fixed_neon.cpp:501-526).
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      acc[J] = 0x00800080u + tp.y[R] * lane_reg<J>(win[(ROT + R) % K]);
+    });
+    static_for<0, R>([&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      static_for<0, 8>([&](auto jc) {
+        constexpr int J = decltype(jc)::value;
+        acc[J] += tp.y[I] * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
       });
-      v[J] = (acc >> 8) & 0x00FF00FFu;
-    } else if constexpr (MODE == MODE_BINOM || MODE == MODE_BLURDOWN) {
-      using B = Binomial<(MODE == MODE_BLURDOWN ? 5 : K)>;
-      acc = B::c(R) * lane_reg<J>(win[(ROT + R) % K]);
-      static_for<0, R>([&](auto ic) {
-        constexpr int I = decltype(ic)::value;
-        acc += B::c(I) * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
+    });
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      v[J] = __byte_perm(acc[J], 0u, 0x4341);  // (acc >> 8) & 0x00FF00FF
+    });
+  } else if constexpr (MODE == MODE_BINOM || MODE == MODE_BLURDOWN) {
+    using B = Binomial<(MODE == MODE_BLURDOWN ? 5 : K)>;
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      acc[J] = B::c(R) * lane_reg<J>(win[(ROT + R) % K]);
+    });
+    static_for<0, R>([&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      static_for<0, 8>([&](auto jc) {
+        constexpr int J = decltype(jc)::value;
+        acc[J] += B::c(I) * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
       });
-      v[J] = acc;  // exact, <= 255 * 256
-    } else {       // MODE_SEP_U8: saturating u16 in the reference; any lane that
-                   // reaches 255 forces a 255 output (taps are non-negative), so
-                   // clamping every product and the sum to 255 gives the same bytes.
-      acc = 0;
-      static_for<0, K>([&](auto tc) {
-        constexpr int T = decltype(tc)::value;
-        acc += vmin_u16x2(tp.y[T] * lane_reg<J>(win[(ROT + T) % K]), 0x00FF00FFu);
+    });
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      v[J] = acc[J];  // exact, <= 255 * 256
+    });
+  } else {  // MODE_SEP_U8: saturating u16 in the reference; any lane that
+            // reaches 255 forces a 255 output (taps are non-negative), so
+            // clamping every product and the sum to 255 gives the same bytes.
+    static_for<0, 8>([&](auto jc) { acc[decltype(jc)::value] = 0; });
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      static_for<0, 8>([&](auto jc) {
+        constexpr int J = decltype(jc)::value;
+        acc[J] += vmin_u16x2(tp.y[T] * lane_reg<J>(win[(ROT + T) % K]), 0x00FF00FFu);
       });
-      v[J] = vmin_u16x2(acc, 0x00FF00FFu);
-    }
-  });
+    });
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      v[J] = vmin_u16x2(acc[J], 0x00FF00FFu);
+    });
+  }
 }
 
 template <int K, int ROT>
@@ -366,6 +378,28 @@ __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const u
     hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
   }
   uint32_t out[4];
+  if constexpr (MODE == MODE_SIGMA) {
+    // Taps outer, the eight lane pairs inner: independent accumulation chains.
+    // Gaussian kernels are identical in both directions: reuse tp.y.
+    uint32_t acc[8];
+    static_for<0, 8>([&](auto jc) {
+      constexpr int J = decltype(jc)::value;
+      acc[J] = 0x00800080u + tp.y[R] * pair_at<HW, NW, J / 2, J % 2, 0>(lo, hi);
+    });
+    static_for<1, R + 1>([&](auto dc) {
+      constexpr int D = decltype(dc)::value;
+      static_for<0, 8>([&](auto jc) {
+        constexpr int J = decltype(jc)::value;
+        acc[J] += tp.y[R - D] * (pair_at<HW, NW, J / 2, J % 2, -D * C>(lo, hi) +
+                                 pair_at<HW, NW, J / 2, J % 2, D * C>(lo, hi));
+      });
+    });
+    static_for<0, 4>([&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      out[I] = __byte_perm(acc[2 * I], acc[2 * I + 1], 0x7351);  // high byte of each lane
+    });
+    return make_uint4(out[0], out[1], out[2], out[3]);
+  }
   static_for<0, 4>([&](auto ic) {
     constexpr int I = decltype(ic)::value;
     uint32_t res[2];
@@ -513,14 +547,14 @@ __device__ __forceinline__ uint2 horizontal_blurdown(const uint32_t *vlo_s, cons
 }
 
 // ---------------------------------------------------------------------------
-// CTA organisation.  `warps` consumer warps each own 32 consecutive chunks
-// (16 bytes of a row per lane): an interior of 32 - 2*HC chunks plus HC halo
-// chunks on either side, which overlap the neighbouring warps' interiors.  A
-// warp therefore needs no other warp's data and synchronises only with
-// __syncwarp; the warps of a CTA share the TMA ring, fed by one extra
-// producer warp through full/empty mbarrier pairs.
+// CTA organisation.  Each warp owns 32 consecutive chunks (16 bytes of a row
+// per lane): an interior of 32 - 2*HC chunks plus HC halo chunks on either
+// side, which overlap the neighbouring warps' interiors.  A warp therefore
+// needs no other warp's data and synchronises only with __syncwarp; the warps
+// of a CTA share the TMA ring through full/empty mbarrier pairs, and lane 0 of
+// warp 0 issues the copies between its own blocks of rows.
 struct CtaShape {
-  int warps;        // consumer warps
+  int warps;        // warps of the CTA
   int wi;           // interior chunks per warp
   int span_chunks;  // chunks of a row the CTA reads: warps * wi + 2 * HC
   int boxes;        // span boxes per row
@@ -530,7 +564,7 @@ struct CtaShape {
 __host__ __device__ inline CtaShape cta_shape(int threads, int hc, int lbw) {
   CtaShape s;
   const int bw = 1 << lbw;
-  s.warps = threads / 32 - 1;
+  s.warps = threads / 32;
   s.wi = 32 - 2 * hc;
   s.span_chunks = s.warps * s.wi + 2 * hc;
   s.boxes = (s.span_chunks * kChunk + bw - 1) / bw;
@@ -545,13 +579,20 @@ __host__ __device__ constexpr uint32_t vrow_bytes_per_lane() {
 }
 
 struct SmemLayout {
-  uint32_t ring_stage_bytes, span_area, v_off, v_warp_bytes, bar_off, total;
+  uint32_t ring_stage_bytes, span_area, edge_off, edge_warp_bytes, v_off, v_warp_bytes, bar_off,
+      total;
 };
+
+// Chunks per warp that can hang over the image's left/right edge and are
+// rebuilt in a per-warp edge area: at most HC on the left plus HC + 1 on the
+// right.
+__host__ __device__ constexpr int edge_slots(int hc) { return 2 * hc + 1; }
 
 // A ring stage holds stage_rows rows.  With TMA: the staged span laid out as
 // [box][row][box bytes] followed by two 256-byte-wide wrap areas
 // ([area][row][256 B]) that receive the far end of the row when a WRAP border
-// needs it.  Without TMA every lane owns a private 16-byte slot per row
+// needs it; chunks hanging over the left/right edge are rebuilt in the edge
+// area.  Without TMA every lane owns a private 16-byte slot per row
 // ([warp][row][32 x 16 B]).
 template <int MODE>
 __host__ __device__ inline SmemLayout smem_layout(int threads, int hc, int lbw, int stage_rows,
@@ -561,7 +602,11 @@ __host__ __device__ inline SmemLayout smem_layout(int threads, int hc, int lbw, 
   const uint32_t tma_row = s.span_bytes + 512, own_row = s.warps * 32 * kChunk;
   l.span_area = static_cast<uint32_t>(stage_rows) * s.span_bytes;
   l.ring_stage_bytes = static_cast<uint32_t>(stage_rows) * (tma_row > own_row ? tma_row : own_row);
-  l.v_off = l.ring_stage_bytes * stages;
+  // Edge area: [warp][stage][row][edge_slots x 16 B], written only by generic
+  // stores (never by TMA), so it needs no proxy fence.
+  l.edge_off = l.ring_stage_bytes * stages;
+  l.edge_warp_bytes = static_cast<uint32_t>(stages) * stage_rows * edge_slots(hc) * kChunk;
+  l.v_off = l.edge_off + s.warps * l.edge_warp_bytes;
   l.v_warp_bytes = 2 * 32 * vrow_bytes_per_lane<MODE>();  // double-buffered
   l.bar_off = l.v_off + s.warps * l.v_warp_bytes;
   l.total = l.bar_off + 16 * stages;  // full[stages] + empty[stages]
@@ -610,6 +655,10 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const long wcb = wc * ES;
   const bool use_tma = j.use_tma != 0;
   const int nstages = (in_rows + rb - 1) >> lrb;
+  // The producer is lane 0 of a warp whose chunks never hang over a strip's
+  // left edge (warp 1 when the CTA has three or more warps): edge warps
+  // already carry the cooperative border patching.
+  const int pw = sh.warps >= 3 ? 1 : 0;
 
   SpanGeo sg;
   sg.xs = xs;
@@ -629,83 +678,87 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     sg.wrapl_x = wcb - hb > 0 ? ((wcb - hb) & ~15L) : 0;
   }
 
-  // ======================= producer warp =======================
-  if (warp == sh.warps) {
-    if (use_tma && lane == 0) {
-      const int bw = 1 << lbw, unit_shift = lbw - 8;  // span map unit = 1 << unit_shift bytes
-      // fn(map, x in map units, destination, row-box) for every box of a stage.
-      auto for_each_box = [&](uint8_t *base, bool single_row, auto &&fn) {
-        for (int b = 0; b < sh.boxes; ++b) {
-          const long x = xs + static_cast<long>(b) * bw;
-          if (x < wcb && x + bw > 0)
-            fn(single_row ? maps.span_row : maps.span, x >> unit_shift, base + b * rb * bw,
-               static_cast<uint32_t>(bw));
-        }
-        uint8_t *wrap = base + L.span_area;
-        if (sg.wrap_left) fn(single_row ? maps.wrap_row : maps.wrap, sg.wrapl_x, wrap, 256u);
-        if (sg.wrap_right) fn(single_row ? maps.wrap_row : maps.wrap, 0L, wrap + rb * 256, 256u);
-      };
-      for (int s = 0; s < nstages && !timed_out; ++s) {
-        const uint32_t g = gstage + s;
-        const int slot = static_cast<int>(g & (ns - 1));
-        const uint32_t use = g >> lns;
-        if (use > 0 && !mbar_wait_bounded(&empty[slot], (use - 1) & 1u, kWaitLimitNs)) {
-          timed_out = true;
-          atomicOr(err_flag, 1);
-          break;
-        }
-        uint8_t *base = ring + slot * L.ring_stage_bytes;
-        uint64_t *bar = &full[slot];
-        // Rows inside the image arrive as stage_rows-high boxes; a stage that
-        // reaches outside gets one single-row box per row of its border-mapped
-        // source row instead (none for a CONSTANT border).
-        const int y = iy0 + s * rb;
-        const bool rows_in = y >= 0 && y + rb <= j.height;
-        uint32_t tx = 0;
-        if (rows_in) {
-          for_each_box(base, false, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) {
-            tx += w * rb;
+  // ======================= producer (lane 0 of warp 0) =======================
+  // fn(map, x in map units, destination, box width) for every box of a stage.
+  const int bw = 1 << lbw, unit_shift = lbw - 8;  // span map unit = 1 << unit_shift bytes
+  auto for_each_box = [&](uint8_t *base, bool single_row, auto &&fn) {
+    for (int b = 0; b < sh.boxes; ++b) {
+      const long x = xs + static_cast<long>(b) * bw;
+      if (x < wcb && x + bw > 0)
+        fn(single_row ? maps.span_row : maps.span, x >> unit_shift, base + b * rb * bw,
+           static_cast<uint32_t>(bw));
+    }
+    uint8_t *wrap = base + L.span_area;
+    if (sg.wrap_left) fn(single_row ? maps.wrap_row : maps.wrap, sg.wrapl_x, wrap, 256u);
+    if (sg.wrap_right) fn(single_row ? maps.wrap_row : maps.wrap, 0L, wrap + rb * 256, 256u);
+  };
+  // Copies stage s into its slot (the slot must be free).  Rows inside the
+  // image arrive as stage_rows-high boxes; a stage that reaches outside gets
+  // one single-row box per row of its border-mapped source row instead (none
+  // for a CONSTANT border).
+  auto issue_stage = [&](int s) {
+    const uint32_t g = gstage + s;
+    const int slot = static_cast<int>(g & (ns - 1));
+    uint8_t *base = ring + slot * L.ring_stage_bytes;
+    uint64_t *bar = &full[slot];
+    const int y = iy0 + s * rb;
+    const bool rows_in = y >= 0 && y + rb <= j.height;
+    uint32_t tx = 0;
+    if (rows_in) {
+      for_each_box(base, false, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w * rb; });
+    } else {
+      for (int r = 0; r < rb; ++r)
+        if (map_index(y + r, j.height, j.border) >= 0)
+          for_each_box(base, true, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w; });
+    }
+    if (tx == 0) {
+      mbar_arrive(bar);
+      return;
+    }
+    mbar_arrive_expect_tx(bar, tx);
+    if (rows_in) {
+      for_each_box(base, false, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
+        tma_load_2d(d, m, static_cast<int>(x), y, bar);
+      });
+    } else {
+      for (int r = 0; r < rb; ++r) {
+        const int my = map_index(y + r, j.height, j.border);
+        if (my >= 0)
+          for_each_box(base, true, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t w) {
+            tma_load_2d(d + r * w, m, static_cast<int>(x), my, bar);
           });
-        } else {
-          for (int r = 0; r < rb; ++r)
-            if (map_index(y + r, j.height, j.border) >= 0)
-              for_each_box(base, true, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) {
-                tx += w;
-              });
-        }
-        if (tx == 0) {
-          mbar_arrive(bar);
-          continue;
-        }
-        mbar_arrive_expect_tx(bar, tx);
-        if (rows_in) {
-          for_each_box(base, false, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
-            tma_load_2d(d, m, static_cast<int>(x), y, bar);
-          });
-        } else {
-          for (int r = 0; r < rb; ++r) {
-            const int my = map_index(y + r, j.height, j.border);
-            if (my >= 0)
-              for_each_box(base, true, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t w) {
-                tma_load_2d(d + r * w, m, static_cast<int>(x), my, bar);
-              });
-          }
-        }
-      }
-      if (timed_out) {
-        // Give copies already issued a bounded time to land before the CTA's
-        // shared memory can be reused.
-        for (int s = 0; s < nstages; ++s) {
-          const uint32_t g = gstage + s;
-          mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs);
-        }
       }
     }
-    gstage += nstages;
-    return;
-  }
+  };
+  // Called by warp pw between its blocks: issues every stage up to
+  // `last_needed` (waiting, with a time limit, for its slot to be released),
+  // then as many further stages as have free slots.
+  int issued = 0;
+  auto produce = [&](int last_needed) {
+    if (use_tma && lane == 0) {
+      while (issued < nstages && !timed_out) {
+        const uint32_t g = gstage + issued;
+        const int slot = static_cast<int>(g & (ns - 1));
+        const uint32_t use = g >> lns;
+        if (use > 0) {
+          if (issued <= last_needed) {
+            if (!mbar_wait_bounded(&empty[slot], (use - 1) & 1u, kWaitLimitNs)) {
+              timed_out = true;
+              atomicOr(err_flag, 1);
+              break;
+            }
+          } else if (!mbar_test_wait(&empty[slot], (use - 1) & 1u)) {
+            break;
+          }
+        }
+        issue_stage(issued);
+        ++issued;
+      }
+    }
+    __syncwarp();
+  };
 
-  // ======================= consumer warps =======================
+  // ======================= consumers (every warp) =======================
   const int cidx = warp * sh.wi + lane;  // chunk index within the CTA span
   const long xb = xs + static_cast<long>(cidx) * kChunk;
   const bool chunk_in = xb >= 0 && xb + kChunk <= wcb;
@@ -716,8 +769,8 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const bool dst_rows_aligned =
       ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 15) == 0;
   // This lane writes a whole 16-byte chunk with one vector store.
-  const bool full_store = dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
   const bool stores = emits && active && xb < wcb;
+  const bool full_store = stores && dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
   const uint32_t bv_elem = ES == 1 ? (static_cast<uint32_t>(j.border_value) & 0xFFu)
                                    : (static_cast<uint32_t>(j.border_value) & 0xFFFFu);
   const uint32_t bv_word = ES == 1 ? bv_elem * 0x01010101u : bv_elem * 0x00010001u;
@@ -740,6 +793,16 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
                    (xb >= 16 && xb + 32 <= wcb);
   }
   const unsigned coop_lanes = __ballot_sync(0xffffffffu, active && !self_load_ok);
+  // With TMA, chunks rebuilt by the warp live in the edge area at compact slot
+  // `edge_slot`; every other chunk is read where TMA put it.
+  uint8_t *const edge_warp = smem + L.edge_off + warp * L.edge_warp_bytes;
+  const int edge_slot = __popc(coop_lanes & ((1u << lane) - 1u));
+  const bool from_edge = use_tma && ((coop_lanes >> lane) & 1u);
+  const uint8_t *const lane_ring = from_edge ? edge_warp + edge_slot * kChunk : ring + chunk_off;
+  const int lane_stage_bytes = from_edge ? rb * edge_slots(HC) * kChunk : static_cast<int>(L.ring_stage_bytes);
+  const int lane_row_pitch = from_edge ? edge_slots(HC) * kChunk : row_pitch;
+  // Rows of a CONSTANT border are substituted when read (TMA never fetched them).
+  const bool const_rows = use_tma && j.border == BORDER_CONSTANT;
 
   Taps tp;
   if constexpr (MODE == MODE_SIGMA) {
@@ -754,69 +817,73 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   }
 
   // Readies stage s for this warp.  With TMA: waits for the copies.  Without:
-  // every lane loads its own chunk of each row.  Then the warp jointly fills
-  // the chunks in `coop_lanes` one element per lane (border-mapped elements
-  // from the staged row, or from global memory without TMA), and every lane
-  // fills its chunk in rows lying in a CONSTANT border.  Lanes that share a
-  // chunk with a neighbouring warp write identical bytes.
+  // every lane loads its own chunk of each row.  Rows lying in a CONSTANT
+  // border get the border value in every chunk.  Then the warp jointly fills
+  // the chunks in `coop_lanes`, one (row, element) pair per lane: border-mapped
+  // elements come from the staged row (or, without TMA, every element from
+  // global memory).  Lanes that share a chunk with a neighbouring warp write
+  // identical bytes.
   auto prepare_stage = [&](int s) {
     const uint32_t g = gstage + s;
-    uint8_t *base = ring + static_cast<int>(g & (ns - 1)) * L.ring_stage_bytes;
-    if (use_tma) {
-      if (!timed_out && !mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs)) {
-        timed_out = true;
-        atomicOr(err_flag, 1);
-      }
+    const int slot = static_cast<int>(g & (ns - 1));
+    uint8_t *base = ring + slot * L.ring_stage_bytes;
+    if (use_tma && !timed_out && !mbar_wait_bounded(&full[slot], (g >> lns) & 1u, kWaitLimitNs)) {
+      timed_out = true;
+      atomicOr(err_flag, 1);
     }
-    bool wrote = false;
+    const int rows = min(rb, in_rows - s * rb);
+    if (!use_tma) {
 #pragma unroll 1
-    for (int r = 0; r < rb; ++r) {
-      const int q = s * rb + r;
-      const int iy = iy0 + q;
-      if (q >= in_rows) break;
-      if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) {
-        if (active) *reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch) =
-            make_uint4(bv_word, bv_word, bv_word, bv_word);
-        wrote = true;
-        continue;
-      }
-      const int ry = map_index(iy, j.height, j.border);
-      const uint8_t *grow = j.src + static_cast<int64_t>(ry) * j.src_stride;
-      if (!use_tma && active && self_load_ok) {
-        uint4 v;
-        load_chunk_fast(grow, xb, wcb, v);
-        *reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch) = v;
-      }
-      unsigned m = coop_lanes;
-      while (m) {
-        const int l = __ffs(m) - 1;
-        m &= m - 1;
-        const long xl = (xs + static_cast<long>(warp * sh.wi + l) * kChunk) / ES + lane;
-        if (lane < E) {
-          const bool inside = xl >= 0 && xl < wc;
-          if (!use_tma || !inside) {
-            const long me = inside ? xl : mapped_element<C>(j, xl);
-            uint32_t v;
-            if (me < 0) {
-              v = bv_elem;
-            } else if (use_tma) {
-              v = staged_byte(base, sg, r, me * ES);
-              if (ES == 2) v |= staged_byte(base, sg, r, me * ES + 1) << 8;
-            } else if (ES == 1) {
-              v = __ldg(grow + me);
-            } else {
-              v = __ldg(reinterpret_cast<const uint16_t *>(grow) + me);
-            }
-            uint8_t *dst = base + chunk_offset(l) + r * row_pitch + lane * ES;
-            dst[0] = static_cast<uint8_t>(v);
-            if (ES == 2) dst[1] = static_cast<uint8_t>(v >> 8);
-            wrote = true;
-          }
+      for (int r = 0; r < rows; ++r) {
+        const int iy = iy0 + s * rb + r;
+        uint4 *dst = reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch);
+        if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) {
+          if (active) *dst = make_uint4(bv_word, bv_word, bv_word, bv_word);
+        } else if (active && self_load_ok) {
+          uint4 v;
+          load_chunk_fast(j.src + static_cast<int64_t>(map_index(iy, j.height, j.border)) *
+                                      j.src_stride,
+                          xb, wcb, v);
+          *dst = v;
         }
       }
     }
-    // Order these generic-proxy writes before any later TMA write to the slot.
-    if (use_tma && wrote) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    int k = 0;
+    for (unsigned m = coop_lanes; m; m &= m - 1, ++k) {
+      const int l = __ffs(m) - 1;
+      const int x0 = static_cast<int>((xs + static_cast<long>(warp * sh.wi + l) * kChunk) / ES);
+      uint8_t *lbase = use_tma ? edge_warp + slot * rb * edge_slots(HC) * kChunk + k * kChunk
+                               : base + chunk_offset(l);
+      const int lpitch = use_tma ? edge_slots(HC) * kChunk : row_pitch;
+#pragma unroll 1
+      for (int idx = lane; idx < rows * E; idx += 32) {
+        const int r = idx / E, e = idx % E;
+        const int iy = iy0 + s * rb + r;
+        if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) continue;
+        const int x = x0 + e;
+        const bool inside = x >= 0 && x < static_cast<int>(wc);
+        int me = x;
+        if (!inside) {
+          const int col = x >= 0 ? x / C : -((-x + C - 1) / C);
+          const int mc = map_index(col, j.width, j.border);
+          me = mc < 0 ? -1 : mc * C + (x - col * C);
+        }
+        uint32_t v;
+        if (me < 0) {
+          v = bv_elem;
+        } else if (use_tma) {
+          v = staged_byte(base, sg, r, static_cast<long>(me) * ES);
+          if (ES == 2) v |= staged_byte(base, sg, r, static_cast<long>(me) * ES + 1) << 8;
+        } else {
+          const uint8_t *grow =
+              j.src + static_cast<int64_t>(map_index(iy, j.height, j.border)) * j.src_stride;
+          v = ES == 1 ? __ldg(grow + me) : __ldg(reinterpret_cast<const uint16_t *>(grow) + me);
+        }
+        uint8_t *dst = lbase + r * lpitch + e * ES;
+        dst[0] = static_cast<uint8_t>(v);
+        if (ES == 2) dst[1] = static_cast<uint8_t>(v >> 8);
+      }
+    }
     __syncwarp();
   };
   // Hands stage s back to the producer once every lane of the warp has read it.
@@ -833,46 +900,56 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   int stage_of_block = 0;  // stage of row qb
   int row_of_block = 0;    // qb % rb
 
-  auto load_row = [&](int u, Row &dst_row) {
+  auto load_row = [&](int q, int u, Row &dst_row) {
     // Row qb + u: stage and row within it from the block's base, no division.
     const int r = row_of_block + u;
-    const int s = stage_of_block + (r >> lrb);
-    const uint8_t *base = ring + static_cast<int>((gstage + s) & (ns - 1)) * L.ring_stage_bytes;
-    const uint4 raw =
-        *reinterpret_cast<const uint4 *>(base + chunk_off + (r & (rb - 1)) * row_pitch);
+    const int slot = static_cast<int>((gstage + stage_of_block + (r >> lrb)) & (ns - 1));
+    uint4 raw = *reinterpret_cast<const uint4 *>(lane_ring + slot * lane_stage_bytes +
+                                                 (r & (rb - 1)) * lane_row_pitch);
+    if (const_rows) {
+      const int iy = iy0 + q;
+      if (iy < 0 || iy >= j.height) raw = make_uint4(bv_word, bv_word, bv_word, bv_word);
+    }
     unpack_row<MODE, K>(raw, dst_row);
   };
+
+  // Hoisted per-tile values used by every emitted row.
+  uint8_t *const dst_base = j.dst;
+  const int64_t dst_stride = j.dst_stride;
+  // Lanes outside the interior compute a duplicate of their nearest interior
+  // neighbour's horizontal pass (never stored), so that no branch is needed.
+  const int hlane = min(max(lane, HC), 31 - HC);
+  const bool partial_store = stores && !full_store;
 
   auto emit = [&](auto rot_c, int q) {
     constexpr int ROT = decltype(rot_c)::value;
     uint32_t *vbuf = vwarp + (emitted & 1) * kVRowWords;
-    // ---- vertical pass -> the warp's shared row
-    if (active) {
-      if constexpr (ModeTraits<MODE>::LANES) {
-        uint32_t v[8];
-        vertical_lanes<MODE, K, ROT>(win, tp, v);
-        *reinterpret_cast<uint4 *>(vbuf + 4 * lane) = make_uint4(v[0], v[1], v[2], v[3]);
-        *reinterpret_cast<uint4 *>(vbuf + 128 + 4 * lane) = make_uint4(v[4], v[5], v[6], v[7]);
-      } else if constexpr (MODE == MODE_SEP_U16) {
-        uint32_t v[8];
-        vertical_u16<K, ROT>(win, tp, v);
-        *reinterpret_cast<uint4 *>(vbuf + 4 * lane) =
-            make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16),
-                       v[6] | (v[7] << 16));
-      } else {
-        int32_t v[8];
-        vertical_s16<K, ROT>(win, tp, v);
-        int32_t *vs = reinterpret_cast<int32_t *>(vbuf);
-        *reinterpret_cast<int4 *>(vs + 8 * lane) = make_int4(v[0], v[1], v[2], v[3]);
-        *reinterpret_cast<int4 *>(vs + 8 * lane + 4) = make_int4(v[4], v[5], v[6], v[7]);
-      }
+    // ---- vertical pass -> the warp's shared row (every lane; lanes past the
+    // right halo hold stale data that no stored result reads)
+    if constexpr (ModeTraits<MODE>::LANES) {
+      uint32_t v[8];
+      vertical_lanes<MODE, K, ROT>(win, tp, v);
+      *reinterpret_cast<uint4 *>(vbuf + 4 * lane) = make_uint4(v[0], v[1], v[2], v[3]);
+      *reinterpret_cast<uint4 *>(vbuf + 128 + 4 * lane) = make_uint4(v[4], v[5], v[6], v[7]);
+    } else if constexpr (MODE == MODE_SEP_U16) {
+      uint32_t v[8];
+      vertical_u16<K, ROT>(win, tp, v);
+      *reinterpret_cast<uint4 *>(vbuf + 4 * lane) =
+          make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16),
+                     v[6] | (v[7] << 16));
+    } else {
+      int32_t v[8];
+      vertical_s16<K, ROT>(win, tp, v);
+      int32_t *vs = reinterpret_cast<int32_t *>(vbuf);
+      *reinterpret_cast<int4 *>(vs + 8 * lane) = make_int4(v[0], v[1], v[2], v[3]);
+      *reinterpret_cast<int4 *>(vs + 8 * lane + 4) = make_int4(v[4], v[5], v[6], v[7]);
     }
     __syncwarp();
     // ---- horizontal pass + store
-    if (emits && active) {
-      const int oy = MODE == MODE_BLURDOWN ? oy0 + (q - 4) / 2 : oy0 + q - (K - 1);
-      uint8_t *drow = j.dst + static_cast<int64_t>(oy) * j.dst_stride;
-      if constexpr (MODE == MODE_BLURDOWN) {
+    const int oy = MODE == MODE_BLURDOWN ? oy0 + (q - 4) / 2 : oy0 + q - (K - 1);
+    uint8_t *drow = dst_base + static_cast<int64_t>(oy) * dst_stride;
+    if constexpr (MODE == MODE_BLURDOWN) {
+      if (emits && active) {
         const long ob = xb / 2;  // destination byte (= element) offset
         const long owc = static_cast<long>(j.out_width) * C;
         if (ob < owc) {
@@ -886,21 +963,20 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
               drow[ob + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
           }
         }
-      } else if (stores) {
-        uint4 r;
-        if constexpr (ModeTraits<MODE>::LANES)
-          r = horizontal_lanes<MODE, K, C>(vbuf, vbuf + 128, lane, tp);
-        else if constexpr (MODE == MODE_SEP_U16)
-          r = horizontal_u16<K, C>(vbuf, lane, tp);
-        else
-          r = horizontal_s16<K, C>(reinterpret_cast<const int32_t *>(vbuf), lane, tp);
-        if (full_store) {
-          st_v4(drow + xb, r);
-        } else {
-          const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
-          for (int k = 0; k < kChunk && xb + k < wcb; ++k)
-            drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
-        }
+      }
+    } else {
+      uint4 r;
+      if constexpr (ModeTraits<MODE>::LANES)
+        r = horizontal_lanes<MODE, K, C>(vbuf, vbuf + 128, hlane, tp);
+      else if constexpr (MODE == MODE_SEP_U16)
+        r = horizontal_u16<K, C>(vbuf, hlane, tp);
+      else
+        r = horizontal_s16<K, C>(reinterpret_cast<const int32_t *>(vbuf), hlane, tp);
+      if (full_store) st_v4(drow + xb, r);
+      if (partial_store) {
+        const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
+        for (int k = 0; k < kChunk && xb + k < wcb; ++k)
+          drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
       }
     }
     ++emitted;
@@ -919,6 +995,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   for (int qb = 0; qb < in_rows; qb += K) {
     const int last_stage = (min(qb + K, in_rows) - 1) >> lrb;
     for (; released < ready && ((released + 1) << lrb) <= qb; ++released) release_stage(released);
+    if (warp == pw) produce(last_stage);
     for (; ready <= last_stage; ++ready) prepare_stage(ready);
     stage_of_block = qb >> lrb;
     row_of_block = qb & (rb - 1);
@@ -926,7 +1003,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
       constexpr int U = decltype(uc)::value;
       const int q = qb + U;
       if (q < in_rows) {
-        load_row(U, win[U]);
+        load_row(q, U, win[U]);
         bool do_emit;
         if constexpr (MODE == MODE_BLURDOWN)
           do_emit = q >= 4 && ((q - 4) & 1) == 0;
@@ -937,13 +1014,22 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     });
   }
   for (; released < nstages; ++released) release_stage(released);
+  if (use_tma && timed_out && warp == pw && lane == 0) {
+    // Give copies already issued a bounded time to land before the CTA's
+    // shared memory can be reused.
+    for (int s2 = 0; s2 < issued; ++s2) {
+      const uint32_t g = gstage + s2;
+      mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs);
+    }
+  }
   gstage += nstages;
 }
 
 // ---------------------------------------------------------------------------
-// Single-image launch: grid (strips, bands), threads = 32 * (warps + 1).
+// Launch: a grid of up to (resident CTAs per SM x SMs) CTAs that walk the
+// job's tiles (strip, band) in row-major band order; threads = 32 * warps.
 template <int MODE, int K, int C>
-__global__ void __launch_bounds__(288, 1) sepfused_kernel(const __grid_constant__ FilterJob job,
+__global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4)) sepfused_kernel(const __grid_constant__ FilterJob job,
                                                           int *err_flag) {
   extern __shared__ __align__(128) uint8_t smem[];
   constexpr int HC = Geo<MODE, K, C>::HC;
@@ -953,10 +1039,10 @@ __global__ void __launch_bounds__(288, 1) sepfused_kernel(const __grid_constant_
       prefetch_tensormap(&job.tmap);
       prefetch_tensormap(&job.tmap_row);
       uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
-      const int consumers = blockDim.x / 32 - 1;
+      const int warps = blockDim.x / 32;
       for (int s = 0; s < job.stages; ++s) {
         mbar_init(&full[s], 1);
-        mbar_init(&full[job.stages + s], consumers);
+        mbar_init(&full[job.stages + s], warps);
       }
       fence_mbar_init();
     }
@@ -965,7 +1051,10 @@ __global__ void __launch_bounds__(288, 1) sepfused_kernel(const __grid_constant_
   uint32_t gstage = 0;
   bool timed_out = false;
   const TmaMaps maps{&job.tmap, &job.tmap_row, &job.tmap_wrap, &job.tmap_wrap_row};
-  run_tile<MODE, K, C>(job, maps, blockIdx.x, blockIdx.y, smem, gstage, err_flag, timed_out);
+  const int tiles = job.strips * job.row_tiles;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x)
+    run_tile<MODE, K, C>(job, maps, t % job.strips, t / job.strips, smem, gstage, err_flag,
+                         timed_out);
 }
 
 }  // namespace kcv
