@@ -373,7 +373,7 @@ def cpu_baseline(calls, passes, outputs=None):
     sec = statistics.median(times)
     return dict(value=round(out_pixels(calls) / sec / 1e6, 2), unit=METRIC, cores=cores, kind="port",
                 sample=f"{passes} full passes of the 7-call sweep (median) with {cores} threads; "
-                       f"CPU restatement oracle/kcv_oracle.c (scalar C, -O2)"), exact
+                       f"CPU restatement oracle/kcv_oracle.c (scalar C, -O3)"), exact
 
 
 # ----------------------------------------------------------------------------
