@@ -291,6 +291,56 @@ double kleidicv_gpu_server_now(const kleidicv_gpu_server_t *server);
 kleidicv_error_t kleidicv_gpu_server_drain(kleidicv_gpu_server_t *server);
 
 /* ------------------------------------------------------------------------ */
+/* Allocation-free arbitrary-size Gaussian.  No counterpart in the reference:
+ * kleidicv_gaussian_blur_u8 (kleidicv.h:2159-2163) allocates its workspace
+ * with malloc on every call (kleidicv/include/kleidicv/workspace/separable.h:82-100).
+ *
+ * For callers that must not allocate device memory on the call path:
+ *  - a process that reserved its whole device budget at start-up;
+ *  - a latency-critical loop, where an allocation (or the device-wide
+ *    synchronisation a cudaFree can imply) is not acceptable;
+ *  - a caller that holds no kleidicv_gpu_context_t (creating one allocates
+ *    its error word).
+ * kleidicv_gpu_gaussian_blur_u8 takes the intermediate image of its two-pass
+ * arbitrary-size kernel from the context's pool on every call.  This entry
+ * takes it from a fixed buffer that is part of the library's device image
+ * (KLEIDICV_GPU_NOALLOC_SCRATCH_BYTES on every device that runs it), and it
+ * calls no allocating routine.
+ *
+ *  - Arguments, validation order and results are those of
+ *    kleidicv_gpu_gaussian_blur_u8, with a cudaStream_t in place of the
+ *    context.
+ *  - It serves the requests that entry computes with the two-pass kernel,
+ *    and those whose kernel is a plain copy.  The two-pass requests are odd
+ *    sizes 11..255 other than 15 and 21 with a REPLICATE border (the
+ *    reference's arbitrary-size path), and generated kernels whose weights
+ *    do not sum to 256.
+ *  - Requests that the fused kernels compute return
+ *    KLEIDICV_ERROR_NOT_IMPLEMENTED.  They need no scratch: call
+ *    kleidicv_gpu_gaussian_blur_u8 with a context created at set-up.
+ *  - Limit: ceil16(width * channels) * height must not exceed
+ *    KLEIDICV_GPU_NOALLOC_SCRATCH_BYTES, otherwise KLEIDICV_ERROR_RANGE.
+ *    This is checked after the drop-in validation.
+ *  - There is one buffer per device.  Calls whose device work can overlap
+ *    race on it and give wrong results: calls on different streams, or from
+ *    several host threads on different streams.  Issue them on one stream,
+ *    or order the streams with events.
+ *  - Nothing has to start at zero: the first kernel writes every scratch
+ *    byte that the second one reads.
+ *  - The first call on each device (with that device current) does a
+ *    one-time set-up.  It resolves the buffer's address
+ *    (cudaGetSymbolAddress) and loads the two kernels, which makes CUDA load
+ *    the library's device code on that device.  Make that first call before
+ *    any stream capture. */
+#define KLEIDICV_GPU_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8_noalloc(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, size_t kernel_width,
+    size_t kernel_height, float sigma_x, float sigma_y,
+    kleidicv_border_type_t border_type, void *stream);
+
+/* ------------------------------------------------------------------------ */
 /* Introspection (used by tests): the Gaussian half kernel this library
  * derives from (kernel_size, sigma), with the reference's generator
  * (kleidicv/include/kleidicv/filters/sigma.h:27-79).  Returns 1 and fills

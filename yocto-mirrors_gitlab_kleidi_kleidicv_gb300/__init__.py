@@ -94,6 +94,8 @@ SIGNATURES = {
     "kleidicv_gpu_server_now": (ctypes.c_double, [_vp]),
     "kleidicv_gpu_server_drain": (_i, [_vp]),
     "kleidicv_gpu_gaussian_half_kernel": (_i, [_sz, _f, ctypes.POINTER(_u8)]),
+    "kleidicv_gpu_gaussian_blur_u8_noalloc": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f,
+                                                   _i, _vp]),
 }
 
 _lib = None
@@ -195,6 +197,14 @@ def gaussian_blur_u8(src, src_stride, dst, dst_stride, width, height, channels, 
     return lib().kleidicv_gpu_gaussian_blur_u8_ex(src, src_stride, dst, dst_stride, width, height,
                                                   channels, kernel_width, kernel_height, sigma_x,
                                                   sigma_y, border_type, border_value, _h(ctx))
+
+
+def gaussian_blur_u8_noalloc(src, src_stride, dst, dst_stride, width, height, channels,
+                             kernel_width, kernel_height, sigma_x, sigma_y, border_type, stream=None):
+    """Allocation-free two-pass Gaussian on a raw cudaStream_t handle (no context)."""
+    return lib().kleidicv_gpu_gaussian_blur_u8_noalloc(src, src_stride, dst, dst_stride, width, height,
+                                                       channels, kernel_width, kernel_height, sigma_x,
+                                                       sigma_y, border_type, stream or None)
 
 
 def separable_filter_2d(dtype, src, src_stride, dst, dst_stride, width, height, channels, kernel_x,

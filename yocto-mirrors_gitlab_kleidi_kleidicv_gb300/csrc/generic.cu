@@ -134,4 +134,11 @@ cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch, siz
   return cudaGetLastError();
 }
 
+cudaError_t preload_generic_gaussian() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, generic_vertical);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, generic_horizontal);
+  return e;
+}
+
 }  // namespace kcv

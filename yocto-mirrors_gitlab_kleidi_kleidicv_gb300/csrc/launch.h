@@ -37,4 +37,8 @@ bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *
 cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch,
                                     size_t scratch_stride, cudaStream_t stream);
 
+// Loads the two generic kernels on the current device (cudaFuncGetAttributes),
+// so that later launches do not trigger CUDA's lazy module loading.
+cudaError_t preload_generic_gaussian();
+
 }  // namespace kcv
