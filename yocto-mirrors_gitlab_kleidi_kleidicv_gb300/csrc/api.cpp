@@ -219,6 +219,20 @@ kleidicv_error_t prepare_separable(int elem, const void *src, size_t src_stride,
       j.wy[t] = static_cast<const int16_t *>(kernel_y)[t];
     }
   }
+  // Narrow taps: no intermediate sum can leave the accumulator width, so the
+  // kernel may add without per-product saturation (identical results).
+  //   u8:  every 16-bit lane sum <= 255 * sum(taps) <= 65535 in both passes;
+  //   u16: every u32 sum <= 65535 * sum(taps) < 2^32 in both passes;
+  //   s16: |vertical| <= 32768 * sum|ky| and |horizontal| <= 32768 *
+  //        sum|kx| * sum|ky| < 2^31, so no saturating add ever saturates.
+  long sx = 0, sy = 0;
+  for (int t = 0; t < 5; ++t) {
+    sx += j.wx[t] < 0 ? -static_cast<long>(j.wx[t]) : j.wx[t];
+    sy += j.wy[t] < 0 ? -static_cast<long>(j.wy[t]) : j.wy[t];
+  }
+  if (elem == 1) j.narrow = sx <= 257 && sy <= 257;
+  else if (elem == 2) j.narrow = sx <= 65537 && sy <= 65537;
+  else j.narrow = sy <= 65535 && sx * sy <= 65535;
   return KLEIDICV_OK;
 }
 
@@ -273,20 +287,28 @@ TileShape tile_shape_for(const FilterJob &j, int sm_count) {
   return t;
 }
 
-// Ring depth rule: stages * stage_rows >= K - 1 + 2 * stage_rows, so that a
+// Ring depth rule: a block of output rows reads block_in_rows consecutive
+// source rows, which touch at most floor((stage_rows - 1 + in_rows - 1) /
+// stage_rows) + 1 stages; the ring holds at least that many stages, so a
 // consumer warp never waits for a stage that cannot be issued until a warp
-// behind it releases one; both counts are powers of two.
+// behind it releases one.  Both counts are powers of two and the ring has at
+// most 16 stages (the mbarrier area), so large kernels get taller stages.
 static void fix_ring(FilterJob &j) {
   auto pow2 = [](int v) {
     int p = 1;
     while (p < v) p <<= 1;
     return p;
   };
-  j.stage_rows = std::max(1, std::min(pow2(j.stage_rows), 64));
-  const int k_rows = j.mode == MODE_BLURDOWN ? 5 : j.ksize;
-  int ns = pow2(std::max(2, j.stages));
-  while (ns * j.stage_rows < k_rows - 1 + 2 * j.stage_rows) ns <<= 1;
-  j.stages = ns;
+  const int in_rows = block_in_rows(j.mode, j.ksize);
+  int rb = std::max(1, std::min(pow2(j.stage_rows), 64));
+  int ns = 0;
+  for (;; rb <<= 1) {
+    const int need = (rb - 1 + in_rows - 1) / rb + 1;
+    ns = pow2(std::max({2, j.stages, need}));
+    if (ns <= 16 || rb >= 64) break;
+  }
+  j.stage_rows = rb;
+  j.stages = std::min(ns, 16);
 }
 
 void apply_tile_shape(FilterJob &j, const TileShape &t) {
@@ -319,6 +341,9 @@ void finish_plan(FilterJob &j, int sm_count) {
     const long target = static_cast<long>(occ) * std::max(sm_count, 1);
     const long bands = std::max(1L, target / std::max<long>(j.strips, 1));
     int rows = static_cast<int>((j.out_height + bands - 1) / bands);
+    // Whole blocks of output rows per tile.
+    const int m = block_out_rows(j.mode, j.ksize);
+    rows = (rows + m - 1) / m * m;
     j.tile_rows = std::max(8, std::min(rows, 1 << 20));
   }
   j.row_tiles = (j.out_height + j.tile_rows - 1) / j.tile_rows;

@@ -5,10 +5,9 @@ bool launch_fused_blurdown(const FilterJob &j, int *e, cudaStream_t s, cudaError
   return dispatch_channels<MODE_BLURDOWN, 5>(j, e, s, out, o);
 }
 size_t fused_smem_bytes(const FilterJob &job) {
-  switch (job.mode) {
-    case MODE_SEP_U16: return smem_layout<MODE_SEP_U16>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages).total;
-    default: return smem_layout<MODE_SIGMA>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages).total;
-  }
+  return smem_layout(job.mode, job.ksize, job.threads, job.halo_chunks, job.box_lbw,
+                     job.stage_rows, job.stages, job.use_tma != 0, job.border == BORDER_WRAP)
+      .total;
 }
 static bool dispatch_fused(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
                            int *occ) {

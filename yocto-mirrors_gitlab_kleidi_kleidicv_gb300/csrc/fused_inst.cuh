@@ -9,12 +9,13 @@
 namespace kcv {
 
 // err_flag == nullptr: only report the occupancy in *blocks_per_sm.
-template <int MODE, int K, int C>
+template <int MODE, int K, int C, bool NARROW>
 cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
                        int *blocks_per_sm = nullptr) {
-  const SmemLayout L =
-      smem_layout<MODE>(job.threads, job.halo_chunks, job.box_lbw, job.stage_rows, job.stages);
-  auto kern = sepfused_kernel<MODE, K, C>;
+  const SmemLayout L = smem_layout(MODE, K, job.threads, job.halo_chunks, job.box_lbw,
+                                   job.stage_rows, job.stages, job.use_tma != 0,
+                                   job.border == BORDER_WRAP);
+  auto kern = sepfused_kernel<MODE, K, C, NARROW>;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -38,16 +39,27 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
   return cudaGetLastError();
 }
 
+template <int MODE, int K, bool NARROW>
+bool dispatch_channels_n(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
+                         int *blocks_per_sm) {
+  switch (job.channels) {
+    case 1: *out = launch_one<MODE, K, 1, NARROW>(job, err, s, blocks_per_sm); return true;
+    case 2: *out = launch_one<MODE, K, 2, NARROW>(job, err, s, blocks_per_sm); return true;
+    case 3: *out = launch_one<MODE, K, 3, NARROW>(job, err, s, blocks_per_sm); return true;
+    case 4: *out = launch_one<MODE, K, 4, NARROW>(job, err, s, blocks_per_sm); return true;
+  }
+  return false;
+}
+
+// Separable modes have a narrow-tap instantiation (job.narrow); the Gaussian
+// and blur-and-downsample arithmetic is narrow by construction.
 template <int MODE, int K>
 bool dispatch_channels(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
                        int *blocks_per_sm = nullptr) {
-  switch (job.channels) {
-    case 1: *out = launch_one<MODE, K, 1>(job, err, s, blocks_per_sm); return true;
-    case 2: *out = launch_one<MODE, K, 2>(job, err, s, blocks_per_sm); return true;
-    case 3: *out = launch_one<MODE, K, 3>(job, err, s, blocks_per_sm); return true;
-    case 4: *out = launch_one<MODE, K, 4>(job, err, s, blocks_per_sm); return true;
+  if constexpr (MODE == MODE_SEP_U8 || MODE == MODE_SEP_U16 || MODE == MODE_SEP_S16) {
+    if (job.narrow) return dispatch_channels_n<MODE, K, true>(job, err, s, out, blocks_per_sm);
   }
-  return false;
+  return dispatch_channels_n<MODE, K, false>(job, err, s, out, blocks_per_sm);
 }
 
 }  // namespace kcv

@@ -29,6 +29,21 @@ enum Border : int32_t {
 constexpr int kMaxTaps = 21;  // largest fused kernel size
 constexpr int kChunk = 16;    // bytes of one row owned by one thread
 
+#ifdef __CUDACC__
+#define KCV_HD __host__ __device__
+#else
+#define KCV_HD
+#endif
+
+// The fused kernel produces output rows in blocks: block_out_rows(mode, k)
+// destination rows from block_in_rows(mode, k) consecutive source rows.
+KCV_HD constexpr int block_out_rows(int mode, int k) {
+  return mode == MODE_BLURDOWN ? 2 : (k >= 15 ? 2 : 4);
+}
+KCV_HD constexpr int block_in_rows(int mode, int k) {
+  return mode == MODE_BLURDOWN ? 2 * block_out_rows(mode, k) + 3 : block_out_rows(mode, k) + k - 1;
+}
+
 struct FilterJob {
   // TMA views of src (valid when use_tma).  The span maps count the row in
   // units of 1 << (box_lbw - 8) bytes (1, or 8 when rows are a multiple of 8
@@ -49,6 +64,10 @@ struct FilterJob {
   int32_t mode;
   int32_t ksize;
   int32_t use_tma;
+  // Separable filters: the taps bound every sum so that plain 32-bit (u16,
+  // s16) or 16-bit-lane (u8) accumulation cannot overflow, so the
+  // saturation of the reference can only act on the final sums.
+  int32_t narrow;
   // Taps of the full kernel: wy vertical, wx horizontal.
   int32_t wy[kMaxTaps];
   int32_t wx[kMaxTaps];

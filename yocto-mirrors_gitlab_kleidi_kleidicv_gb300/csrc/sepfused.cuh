@@ -13,14 +13,14 @@
 //     the row, and chunks hanging over the left/right edge gather their
 //     mapped elements from shared memory.  Sources that TMA cannot address
 //     (unaligned base or stride) are read with plain loads instead;
-//   * each thread keeps the last K rows of its chunk in registers (a sliding
-//     window rotated by unrolling, so no register moves), and computes the
-//     vertical pass on packed 16-bit lanes in the reference's intermediate
-//     width and rounding;
-//   * the vertical row goes to a double-buffered shared row, one barrier,
-//     then the horizontal pass reads its neighbours' lanes at compile-time
-//     offsets (tap distance = channels elements) and the result is stored
-//     with 16-byte stores.
+//   * output rows are produced in blocks of M: each thread reads the M+K-1
+//     source rows of its chunk from the ring once, unpacks each once (u8 as
+//     packed 16-bit lanes) and adds it into the M vertical sums it belongs
+//     to, in the reference's intermediate width and rounding;
+//   * the M vertical rows go to the warp's shared V rows, then the
+//     horizontal pass reads its neighbours' lanes at compile-time offsets
+//     (tap distance = channels elements) one output row at a time, and the
+//     result is stored with 16-byte stores.
 //
 // Every output byte equals the reference's: the arithmetic per mode follows
 // kleidicv/src/filters/gaussian_blur_fixed_neon.cpp (binomial 3/5/7/9 and
@@ -66,7 +66,6 @@ struct Geo {
   static constexpr int HC = (HALO_ELEMS * ES + kChunk - 1) / kChunk;  // halo chunks / side
   static constexpr int HW = 4 * HC;                                   // halo words / side
   static constexpr int NW = 4 + 2 * HW;  // 32-bit words read around a chunk
-  static constexpr bool PACKED = ModeTraits<MODE>::LANES && K >= 15;
 };
 
 // ---------------------------------------------------------------------------
@@ -113,100 +112,39 @@ __device__ __forceinline__ bool load_chunk_fast(const uint8_t *row, long xb, lon
   return true;
 }
 
-// Where the bytes of one tile row live in a ring stage.
-struct SpanGeo {
+// Where the bytes of the tile rows live in shared memory.  The ring holds
+// ring_rows = stages * stage_rows rows; stage s of a tile occupies ring rows
+// [slot * stage_rows, slot * stage_rows + stage_rows) with slot = (g + s) mod
+// stages, so tile row q (global stage counter g) is ring row
+// (g * stage_rows + q) mod ring_rows.  With TMA the span is laid out as
+// [box][ring row][box bytes] (every box of a stage-rows-high TMA copy lands
+// on consecutive ring rows), the two wrap areas as [area][ring row][256 B].
+struct RingGeo {
   long xs;        // first byte of the span (multiple of 16, may be negative)
   long span_end;  // xs + boxes * box bytes
   long wcb;       // bytes per image row
   long wrapl_x;   // first byte of the left wrap area's box (valid if wrap_left)
   int lbw;        // log2 of the span box width in bytes (256 or 2048)
-  int rb;         // rows per stage
-  int span_area;  // bytes of a stage taken by the span boxes
+  int ring_rows;  // rows in the ring (power of two)
   bool wrap_left, wrap_right;
 };
 
-// Offset within a stage of byte `o` of the span in row r ([box][row][box bytes]).
-__device__ __forceinline__ int span_offset(const SpanGeo &g, int r, int o) {
-  const int bw = 1 << g.lbw;
-  return (o >> g.lbw) * g.rb * bw + r * bw + (o & (bw - 1));
-}
-
-// Byte `b` (absolute offset within the image row) of stage row `r`, from the
+// Byte `b` (absolute offset within the image row) of ring row `rr`, from the
 // span or a wrap area.  Bytes that were not staged read as 0; only halo lanes
 // whose results are discarded can ask for them.
-__device__ __forceinline__ uint32_t staged_byte(const uint8_t *slot, const SpanGeo &g, int r,
-                                                long b) {
-  if (b >= g.xs && b < g.span_end) return slot[span_offset(g, r, static_cast<int>(b - g.xs))];
-  const uint8_t *wrap = slot + g.span_area;
-  if (g.wrap_left && b >= g.wrapl_x && b < g.wrapl_x + 256) return wrap[r * 256 + (b - g.wrapl_x)];
-  if (g.wrap_right && b >= 0 && b < 256) return wrap[g.rb * 256 + r * 256 + b];
+__device__ __forceinline__ uint32_t staged_byte(const uint8_t *ring, const uint8_t *wrap,
+                                                const RingGeo &g, int rr, long b) {
+  const int bw = 1 << g.lbw;
+  if (b >= g.xs && b < g.span_end) {
+    const int o = static_cast<int>(b - g.xs);
+    return ring[(o >> g.lbw) * g.ring_rows * bw + rr * bw + (o & (bw - 1))];
+  }
+  if (g.wrap_left && b >= g.wrapl_x && b < g.wrapl_x + 256) return wrap[rr * 256 + (b - g.wrapl_x)];
+  if (g.wrap_right && b >= 0 && b < 256) return wrap[(g.ring_rows + rr) * 256 + b];
   return 0;
 }
 
 // ---------------------------------------------------------------------------
-// Per-thread row representations.
-struct LaneRow {  // 16 u8 elements as 16-bit lanes: lo = elements 4i, 4i+2; hi = 4i+1, 4i+3
-  uint32_t lo[4], hi[4];
-};
-struct RawRow {  // 16 raw bytes (packed window for large kernels)
-  uint32_t w[4];
-};
-struct U32Row {  // 8 u16 elements widened to u32
-  uint32_t e[8];
-};
-struct S32Row {  // 8 s16 elements sign-extended
-  int32_t e[8];
-};
-
-template <int MODE, int K>
-struct RowOf {
-  using type = std::conditional_t<
-      MODE == MODE_SEP_U16, U32Row,
-      std::conditional_t<MODE == MODE_SEP_S16, S32Row,
-                         std::conditional_t<(K >= 15), RawRow, LaneRow>>>;
-};
-
-__device__ __forceinline__ uint32_t lanes_lo(uint32_t w) { return w & 0x00FF00FFu; }
-__device__ __forceinline__ uint32_t lanes_hi(uint32_t w) { return __byte_perm(w, 0u, 0x4341); }
-
-template <int MODE, int K>
-__device__ __forceinline__ void unpack_row(const uint4 &raw, typename RowOf<MODE, K>::type &r) {
-  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
-  using Row = typename RowOf<MODE, K>::type;
-  if constexpr (std::is_same_v<Row, LaneRow>) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      r.lo[i] = lanes_lo(w[i]);
-      r.hi[i] = lanes_hi(w[i]);
-    }
-  } else if constexpr (std::is_same_v<Row, RawRow>) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) r.w[i] = w[i];
-  } else if constexpr (std::is_same_v<Row, U32Row>) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      r.e[2 * i] = w[i] & 0xFFFFu;
-      r.e[2 * i + 1] = w[i] >> 16;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      r.e[2 * i] = static_cast<int32_t>(static_cast<int16_t>(w[i] & 0xFFFFu));
-      r.e[2 * i + 1] = static_cast<int32_t>(w[i]) >> 16;
-    }
-  }
-}
-
-// Lane j (0..7 over lo[0..3], hi[0..3]) of a lane-form or packed row.
-template <int J>
-__device__ __forceinline__ uint32_t lane_reg(const LaneRow &r) {
-  return J < 4 ? r.lo[J & 3] : r.hi[J & 3];
-}
-template <int J>
-__device__ __forceinline__ uint32_t lane_reg(const RawRow &r) {
-  return J < 4 ? lanes_lo(r.w[J & 3]) : lanes_hi(r.w[J & 3]);
-}
-
 // Binomial coefficient sets and rounding shifts of the reference
 // (gaussian_blur_fixed_neon.cpp: 3x3 :27-85, 5x5 :87-153, 7x7 :155-281,
 // 9x9 :283-459).
@@ -240,106 +178,120 @@ struct Binomial<9> {
   static constexpr int shift = 16;
 };
 
-// Taps held in registers for the duration of a tile.
+// Taps held in registers for the duration of a tile.  Gaussian kernels are
+// symmetric: y[0..K/2] only, used in both directions.
 struct Taps {
   uint32_t y[kMaxTaps];
   uint32_t x[kMaxTaps];
 };
 
 // ---------------------------------------------------------------------------
-// Vertical pass over the window.  Tap t lives in slot (ROT + t) % K.
-// Output: lane form (u8 modes), u32 (u16), s32 (s16).
+// A row chunk (16 bytes) in arithmetic form: u8 data as eight words of two
+// 16-bit lanes (x[0..3] = elements 4i, 4i+2; x[4..7] = elements 4i+1, 4i+3),
+// u16 as eight u32, s16 as eight sign-extended s32.
+template <int MODE>
+__device__ __forceinline__ void unpack_chunk(const uint4 &raw, uint32_t (&x)[8]) {
+  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+  if constexpr (ModeTraits<MODE>::LANES) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      x[i] = w[i] & 0x00FF00FFu;
+      x[4 + i] = __byte_perm(w[i], 0u, 0x4341);
+    }
+  } else if constexpr (MODE == MODE_SEP_U16) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      x[2 * i] = w[i] & 0xFFFFu;
+      x[2 * i + 1] = w[i] >> 16;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      x[2 * i] = static_cast<uint32_t>(static_cast<int32_t>(static_cast<int16_t>(w[i] & 0xFFFFu)));
+      x[2 * i + 1] = static_cast<uint32_t>(static_cast<int32_t>(w[i]) >> 16);
+    }
+  }
+}
 
-template <int MODE, int K, int ROT, typename Row>
-__device__ __forceinline__ void vertical_lanes(const Row (&win)[K], const Taps &tp,
-                                               uint32_t (&v)[8]) {
-  constexpr int R = K / 2;
-  // Taps outer, lane registers inner: eight independent accumulation chains.
-  uint32_t acc[8];
+// One vertical tap: acc + weight(T) * x in the mode's intermediate arithmetic.
+template <int MODE, int K, bool NARROW, int T>
+__device__ __forceinline__ uint32_t vtap(uint32_t acc, uint32_t x, const Taps &tp) {
   if constexpr (MODE == MODE_SIGMA) {
-    // (sum + 128) >> 8 kept in 16-bit lanes: the weights sum to 256 so a lane
-    // never exceeds 255*256 + 128 (fixed sizes: gaussian_blur_fixed_neon.cpp:501-526).
-    static_for<0, 8>([&](auto jc) {
-      constexpr int J = decltype(jc)::value;
-      acc[J] = 0x00800080u + tp.y[R] * lane_reg<J>(win[(ROT + R) % K]);
-    });
-    static_for<0, R>([&](auto ic) {
-      constexpr int I = decltype(ic)::value;
-      static_for<0, 8>([&](auto jc) {
-        constexpr int J = decltype(jc)::value;
-        acc[J] += tp.y[I] * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
-      });
-    });
-    static_for<0, 8>([&](auto jc) {
-      constexpr int J = decltype(jc)::value;
-      v[J] = __byte_perm(acc[J], 0u, 0x4341);  // (acc >> 8) & 0x00FF00FF
-    });
-  } else if constexpr (MODE == MODE_BINOM || MODE == MODE_BLURDOWN) {
-    using B = Binomial<(MODE == MODE_BLURDOWN ? 5 : K)>;
-    static_for<0, 8>([&](auto jc) {
-      constexpr int J = decltype(jc)::value;
-      acc[J] = B::c(R) * lane_reg<J>(win[(ROT + R) % K]);
-    });
-    static_for<0, R>([&](auto ic) {
-      constexpr int I = decltype(ic)::value;
-      static_for<0, 8>([&](auto jc) {
-        constexpr int J = decltype(jc)::value;
-        acc[J] += B::c(I) * (lane_reg<J>(win[(ROT + I) % K]) + lane_reg<J>(win[(ROT + K - 1 - I) % K]));
-      });
-    });
-    static_for<0, 8>([&](auto jc) {
-      constexpr int J = decltype(jc)::value;
-      v[J] = acc[J];  // exact, <= 255 * 256
-    });
-  } else {  // MODE_SEP_U8: saturating u16 in the reference; any lane that
-            // reaches 255 forces a 255 output (taps are non-negative), so
-            // clamping every product and the sum to 255 gives the same bytes.
-    static_for<0, 8>([&](auto jc) { acc[decltype(jc)::value] = 0; });
-    static_for<0, K>([&](auto tc) {
-      constexpr int T = decltype(tc)::value;
-      static_for<0, 8>([&](auto jc) {
-        constexpr int J = decltype(jc)::value;
-        acc[J] += vmin_u16x2(tp.y[T] * lane_reg<J>(win[(ROT + T) % K]), 0x00FF00FFu);
-      });
-    });
-    static_for<0, 8>([&](auto jc) {
-      constexpr int J = decltype(jc)::value;
-      v[J] = vmin_u16x2(acc[J], 0x00FF00FFu);
-    });
+    constexpr int H = T <= K / 2 ? T : K - 1 - T;
+    return acc + tp.y[H] * x;  // weights sum to 256: 16-bit lanes never carry
+  } else if constexpr (MODE == MODE_BINOM) {
+    return acc + static_cast<uint32_t>(Binomial<K>::c(T)) * x;  // <= 255 * 256
+  } else if constexpr (MODE == MODE_BLURDOWN) {
+    return acc + static_cast<uint32_t>(Binomial<5>::c(T)) * x;
+  } else if constexpr (MODE == MODE_SEP_U8) {
+    // Saturating u16 in the reference (separable_filter_2d_neon.cpp:38-56).
+    // Taps are non-negative, so any lane reaching 255 forces a 255 output:
+    // clamping products and sum to 255 gives the same bytes; with NARROW taps
+    // (sum <= 257) the plain lane sum cannot carry.
+    if constexpr (NARROW) return acc + tp.y[T] * x;
+    else return acc + vmin_u16x2(tp.y[T] * x, 0x00FF00FFu);
+  } else if constexpr (MODE == MODE_SEP_U16) {
+    // separable_filter_2d_neon.cpp:140-158: saturating u32 sums of u16 x u16
+    // products, then a saturating narrow of the horizontal sum; clamping each
+    // product and the sum to 65535 yields the same outputs (taps >= 0).
+    if constexpr (NARROW) return acc + tp.y[T] * x;
+    else return acc + min(tp.y[T] * x, 0xFFFFu);
+  } else {
+    // s16 extension: saturating s32 adds in tap order.
+    const int32_t p = static_cast<int32_t>(tp.y[T]) * static_cast<int32_t>(x);
+    if constexpr (NARROW) return static_cast<uint32_t>(static_cast<int32_t>(acc) + p);
+    else return static_cast<uint32_t>(add_sat_s32(static_cast<int32_t>(acc), p));
   }
 }
 
-template <int K, int ROT>
-__device__ __forceinline__ void vertical_u16(const U32Row (&win)[K], const Taps &tp,
-                                             uint32_t (&v)[8]) {
-  // separable_filter_2d_neon.cpp:140-158: saturating u32 sums of u16 x u16
-  // products, then a saturating narrow of the horizontal sum.  Clamping each
-  // product and the vertical sum to 65535 yields identical outputs because the
-  // taps are non-negative.
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    uint32_t acc = 0;
-    static_for<0, K>([&](auto tc) {
-      constexpr int T = decltype(tc)::value;
-      acc += min(tp.y[T] * win[(ROT + T) % K].e[e], 0xFFFFu);
-    });
-    v[e] = min(acc, 0xFFFFu);
-  }
+template <int MODE>
+__device__ __forceinline__ uint32_t vfinish(uint32_t acc) {
+  if constexpr (MODE == MODE_SIGMA) return __byte_perm(acc, 0u, 0x4341);  // (acc >> 8) per lane
+  else if constexpr (MODE == MODE_SEP_U8) return vmin_u16x2(acc, 0x00FF00FFu);
+  else if constexpr (MODE == MODE_SEP_U16) return min(acc, 0xFFFFu);
+  else return acc;  // binomial / blur-and-downsample (exact), s16 (s32 bits)
 }
 
-template <int K, int ROT>
-__device__ __forceinline__ void vertical_s16(const S32Row (&win)[K], const Taps &tp,
-                                             int32_t (&v)[8]) {
-  // Extension semantics: tap-0 product, then saturating s32 adds in tap order.
+// Vertical pass of one block: block_out_rows output rows from
+// block_in_rows consecutive ring rows starting at ring row rr0.  Each source
+// row is read from shared memory and unpacked once, then added into every
+// output row it belongs to (taps outer, lanes inner: independent chains).
+// Rows whose bit is set in `cmask` lie in a CONSTANT border and read as the
+// border value.
+template <int MODE, int K, bool NARROW>
+__device__ __forceinline__ void vertical_block(const uint8_t *lane_base, uint32_t pitch,
+                                               uint32_t rr0, uint32_t ring_mask, uint32_t cmask,
+                                               uint32_t bv_word, const Taps &tp,
+                                               uint32_t (&v)[block_out_rows(MODE, K)][8]) {
+  constexpr int M = block_out_rows(MODE, K);
+  constexpr int NIN = block_in_rows(MODE, K);
+  constexpr int KT = MODE == MODE_BLURDOWN ? 5 : K;
+  uint32_t acc[M][8];
+  static_for<0, M>([&](auto mc) {
+    constexpr int Mi = decltype(mc)::value;
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    int32_t acc = static_cast<int32_t>(tp.y[0]) * win[ROT % K].e[e];
-    static_for<1, K>([&](auto tc) {
-      constexpr int T = decltype(tc)::value;
-      acc = add_sat_s32(acc, static_cast<int32_t>(tp.y[T]) * win[(ROT + T) % K].e[e]);
+    for (int j = 0; j < 8; ++j) acc[Mi][j] = MODE == MODE_SIGMA ? 0x00800080u : 0u;
+  });
+  static_for<0, NIN>([&](auto ic) {
+    constexpr int I = decltype(ic)::value;
+    uint4 raw = *reinterpret_cast<const uint4 *>(lane_base + ((rr0 + I) & ring_mask) * pitch);
+    if (cmask & (1u << I)) raw = make_uint4(bv_word, bv_word, bv_word, bv_word);
+    uint32_t x[8];
+    unpack_chunk<MODE>(raw, x);
+    static_for<0, M>([&](auto mc) {
+      constexpr int Mi = decltype(mc)::value;
+      constexpr int T = MODE == MODE_BLURDOWN ? I - 2 * Mi : I - Mi;
+      if constexpr (T >= 0 && T < KT) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[Mi][j] = vtap<MODE, K, NARROW, T>(acc[Mi][j], x[j], tp);
+      }
     });
-    v[e] = acc;
-  }
+  });
+  static_for<0, M>([&](auto mc) {
+    constexpr int Mi = decltype(mc)::value;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[Mi][j] = vfinish<MODE>(acc[Mi][j]);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -362,8 +314,9 @@ __device__ __forceinline__ uint32_t pair_at(const uint32_t (&lo)[NW], const uint
   }
 }
 
-// Computes the 16 output bytes of the thread for lane-form modes.
-template <int MODE, int K, int C>
+// The 16 output bytes of the thread for the lane-form modes.  The V row
+// holds, per lane, its lo words then (128 words later) its hi words.
+template <int MODE, int K, int C, bool NARROW>
 __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const uint32_t *vhi_s,
                                                   int tid, const Taps &tp) {
   using G = Geo<MODE, K, C>;
@@ -377,141 +330,137 @@ __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const u
     lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
     hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
   }
+  // Taps outer, the eight lane pairs (J = 2*I + P) inner.
+  uint32_t acc[8];
   uint32_t out[4];
-  if constexpr (MODE == MODE_SIGMA) {
-    // Taps outer, the eight lane pairs inner: independent accumulation chains.
-    // Gaussian kernels are identical in both directions: reuse tp.y.
-    uint32_t acc[8];
+  if constexpr (MODE == MODE_SIGMA || (MODE == MODE_BINOM && K <= 5)) {
+    // Sums stay inside 16-bit lanes: sigma weights sum to 256, binomial 5x5
+    // to 256 (3x3 to 16) before the rounding shift.
     static_for<0, 8>([&](auto jc) {
       constexpr int J = decltype(jc)::value;
-      acc[J] = 0x00800080u + tp.y[R] * pair_at<HW, NW, J / 2, J % 2, 0>(lo, hi);
+      uint32_t c0;
+      if constexpr (MODE == MODE_SIGMA) c0 = 0x00800080u + tp.y[R] * pair_at<HW, NW, J / 2, J % 2, 0>(lo, hi);
+      else c0 = (1u << (Binomial<K>::shift - 1)) * 0x00010001u +
+                Binomial<K>::c(R) * pair_at<HW, NW, J / 2, J % 2, 0>(lo, hi);
+      acc[J] = c0;
     });
     static_for<1, R + 1>([&](auto dc) {
       constexpr int D = decltype(dc)::value;
       static_for<0, 8>([&](auto jc) {
         constexpr int J = decltype(jc)::value;
-        acc[J] += tp.y[R - D] * (pair_at<HW, NW, J / 2, J % 2, -D * C>(lo, hi) +
-                                 pair_at<HW, NW, J / 2, J % 2, D * C>(lo, hi));
+        const uint32_t pr = pair_at<HW, NW, J / 2, J % 2, -D * C>(lo, hi) +
+                            pair_at<HW, NW, J / 2, J % 2, D * C>(lo, hi);
+        if constexpr (MODE == MODE_SIGMA) acc[J] += tp.y[R - D] * pr;
+        else acc[J] += Binomial<K>::c(R - D) * pr;
       });
     });
     static_for<0, 4>([&](auto ic) {
       constexpr int I = decltype(ic)::value;
-      out[I] = __byte_perm(acc[2 * I], acc[2 * I + 1], 0x7351);  // high byte of each lane
+      if constexpr (MODE == MODE_BINOM && K == 3)
+        out[I] = __byte_perm((acc[2 * I] >> 4) & 0x00FF00FFu, (acc[2 * I + 1] >> 4) & 0x00FF00FFu,
+                             0x6240);
+      else
+        out[I] = __byte_perm(acc[2 * I], acc[2 * I + 1], 0x7351);  // high byte of each lane
     });
-    return make_uint4(out[0], out[1], out[2], out[3]);
-  }
-  static_for<0, 4>([&](auto ic) {
-    constexpr int I = decltype(ic)::value;
-    uint32_t res[2];
-    static_for<0, 2>([&](auto pc) {
-      constexpr int P = decltype(pc)::value;
-      if constexpr (MODE == MODE_SIGMA) {
-        // Gaussian kernels are identical in both directions: reuse tp.y.
-        uint32_t acc = 0x00800080u + tp.y[R] * pair_at<HW, NW, I, P, 0>(lo, hi);
-        static_for<1, R + 1>([&](auto dc) {
-          constexpr int D = decltype(dc)::value;
-          acc += tp.y[R - D] * (pair_at<HW, NW, I, P, -D * C>(lo, hi) +
-                                pair_at<HW, NW, I, P, D * C>(lo, hi));
-        });
-        res[P] = acc;
-      } else if constexpr (MODE == MODE_SEP_U8) {
-        uint32_t acc = 0;
+  } else if constexpr (MODE == MODE_SEP_U8) {
+    static_for<0, 8>([&](auto jc) { acc[decltype(jc)::value] = 0; });
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+      static_for<0, 8>([&](auto jc) {
+        constexpr int J = decltype(jc)::value;
+        const uint32_t p = tp.x[T] * pair_at<HW, NW, J / 2, J % 2, (T - R) * C>(lo, hi);
+        if constexpr (NARROW) acc[J] += p;
+        else acc[J] += vmin_u16x2(p, 0x00FF00FFu);
+      });
+    });
+    static_for<0, 4>([&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      out[I] = __byte_perm(vmin_u16x2(acc[2 * I], 0x00FF00FFu),
+                           vmin_u16x2(acc[2 * I + 1], 0x00FF00FFu), 0x6240);
+    });
+  } else {
+    // Binomial 7x7 / 9x9 need 32-bit sums (u32 in the reference, :220-279, :395-438).
+    using B = Binomial<K>;
+    static_for<0, 4>([&](auto ic) {
+      constexpr int I = decltype(ic)::value;
+      uint32_t res[2];
+      static_for<0, 2>([&](auto pc) {
+        constexpr int P = decltype(pc)::value;
+        uint32_t a0 = 1u << (B::shift - 1), a1 = a0;
         static_for<0, K>([&](auto tc) {
           constexpr int T = decltype(tc)::value;
-          acc += vmin_u16x2(tp.x[T] * pair_at<HW, NW, I, P, (T - R) * C>(lo, hi), 0x00FF00FFu);
+          const uint32_t pr = pair_at<HW, NW, I, P, (T - R) * C>(lo, hi);
+          a0 += B::c(T) * (pr & 0xFFFFu);
+          a1 += B::c(T) * (pr >> 16);
         });
-        res[P] = vmin_u16x2(acc, 0x00FF00FFu);
-      } else {  // MODE_BINOM
-        using B = Binomial<K>;
-        if constexpr (K <= 5) {
-          // Fits 16-bit lanes: 5x5 sums to 255*16*16, 3x3 to 255*4*4.
-          uint32_t acc = (1u << (B::shift - 1)) * 0x00010001u +
-                         B::c(R) * pair_at<HW, NW, I, P, 0>(lo, hi);
-          static_for<1, R + 1>([&](auto dc) {
-            constexpr int D = decltype(dc)::value;
-            acc += B::c(R - D) * (pair_at<HW, NW, I, P, -D * C>(lo, hi) +
-                                  pair_at<HW, NW, I, P, D * C>(lo, hi));
-          });
-          res[P] = acc;
-        } else {
-          // 7x7 / 9x9 need 32-bit sums (u32 in the reference, :220-279, :395-438).
-          uint32_t a0 = 1u << (B::shift - 1), a1 = a0;
-          static_for<0, K>([&](auto tc) {
-            constexpr int T = decltype(tc)::value;
-            const uint32_t pr = pair_at<HW, NW, I, P, (T - R) * C>(lo, hi);
-            a0 += B::c(T) * (pr & 0xFFFFu);
-            a1 += B::c(T) * (pr >> 16);
-          });
-          res[P] = ((a0 >> B::shift) & 0xFFu) | (((a1 >> B::shift) & 0xFFu) << 16);
-        }
-      }
-    });
-    // Pack lanes back to bytes: element order 4I, 4I+1, 4I+2, 4I+3.
-    if constexpr (MODE == MODE_SIGMA || (MODE == MODE_BINOM && K == 5)) {
-      out[I] = __byte_perm(res[0], res[1], 0x7351);  // high byte of each lane
-    } else if constexpr (MODE == MODE_BINOM && K == 3) {
-      out[I] = __byte_perm((res[0] >> 4) & 0x00FF00FFu, (res[1] >> 4) & 0x00FF00FFu, 0x6240);
-    } else {
+        res[P] = ((a0 >> B::shift) & 0xFFu) | (((a1 >> B::shift) & 0xFFu) << 16);
+      });
       out[I] = __byte_perm(res[0], res[1], 0x6240);  // low byte of each lane
-    }
-  });
+    });
+  }
   return make_uint4(out[0], out[1], out[2], out[3]);
 }
 
-// u16 separable: V row is u16 elements (same layout as the input row).
-template <int K, int C>
-__device__ __forceinline__ uint4 horizontal_u16(const uint32_t *v_s, int tid, const Taps &tp) {
-  using G = Geo<MODE_SEP_U16, K, C>;
-  constexpr int R = K / 2, HW = G::HW, NW = G::NW;
-  uint32_t w[NW];
-  const int base = 4 * tid - HW;
-#pragma unroll
-  for (int k = 0; k < NW; k += 4) {
-    const uint4 a = *reinterpret_cast<const uint4 *>(v_s + base + k);
-    w[k] = a.x; w[k + 1] = a.y; w[k + 2] = a.z; w[k + 3] = a.w;
-  }
-  uint32_t o[8];
-  static_for<0, 8>([&](auto ec) {
-    constexpr int E = decltype(ec)::value;
-    uint32_t acc = 0;
-    static_for<0, K>([&](auto tc) {
-      constexpr int T = decltype(tc)::value;
-      constexpr int el = 2 * HW + E + (T - R) * C;  // element index into w (2 per word)
-      static_assert(el >= 0 && el / 2 < NW, "halo too small");
-      const uint32_t val = (el & 1) ? (w[el / 2] >> 16) : (w[el / 2] & 0xFFFFu);
-      acc += min(tp.x[T] * val, 0xFFFFu);
-    });
-    o[E] = min(acc, 0xFFFFu);
-  });
-  return make_uint4(o[0] | (o[1] << 16), o[2] | (o[3] << 16), o[4] | (o[5] << 16),
-                    o[6] | (o[7] << 16));
-}
-
-// s16 separable: V row is s32 elements.
-template <int K, int C>
-__device__ __forceinline__ uint4 horizontal_s16(const int32_t *v_s, int tid, const Taps &tp) {
-  using G = Geo<MODE_SEP_S16, K, C>;
+// u16 / s16 separable: the V row holds 8 32-bit elements per lane (u16
+// values clamped to 65535, or s16 vertical sums), lane-major.
+template <int MODE, int K, int C, bool NARROW>
+__device__ __forceinline__ uint4 horizontal_wide(const uint32_t *v_s, int tid, const Taps &tp) {
+  using G = Geo<MODE, K, C>;
   constexpr int R = K / 2, HE = 2 * G::HW, NE = 8 + 2 * HE;  // elements
-  int32_t v[NE];
+  uint32_t v[NE];
   const int base = 8 * tid - HE;
 #pragma unroll
   for (int k = 0; k < NE; k += 4) {
-    const int4 a = *reinterpret_cast<const int4 *>(v_s + base + k);
+    const uint4 a = *reinterpret_cast<const uint4 *>(v_s + base + k);
     v[k] = a.x; v[k + 1] = a.y; v[k + 2] = a.z; v[k + 3] = a.w;
   }
   uint32_t o[8];
-  static_for<0, 8>([&](auto ec) {
-    constexpr int E = decltype(ec)::value;
-    int64_t acc = 0;
+  if constexpr (MODE == MODE_SEP_U16) {
+    uint32_t acc[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] = 0;
     static_for<0, K>([&](auto tc) {
       constexpr int T = decltype(tc)::value;
-      constexpr int el = HE + E + (T - R) * C;
-      static_assert(el >= 0 && el < NE, "halo too small");
-      acc += static_cast<int64_t>(static_cast<int32_t>(tp.x[T])) * v[el];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const uint32_t p = tp.x[T] * v[HE + e + (T - R) * C];
+        acc[e] += NARROW ? p : min(p, 0xFFFFu);
+      }
     });
-    const int64_t c = acc > 32767 ? 32767 : (acc < -32768 ? -32768 : acc);
-    o[E] = static_cast<uint32_t>(c) & 0xFFFFu;
-  });
+#pragma unroll
+    for (int e = 0; e < 8; ++e) o[e] = min(acc[e], 0xFFFFu);
+  } else if constexpr (NARROW) {
+    // |sum| < 2^31: plain 32-bit accumulation, then saturation to s16.
+    int32_t acc[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] = 0;
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        acc[e] += static_cast<int32_t>(tp.x[T]) * static_cast<int32_t>(v[HE + e + (T - R) * C]);
+    });
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      o[e] = static_cast<uint32_t>(max(-32768, min(acc[e], 32767))) & 0xFFFFu;
+  } else {
+    // s16 extension: 64-bit horizontal accumulation, saturation to s16.
+    int64_t acc[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] = 0;
+    static_for<0, K>([&](auto tc) {
+      constexpr int T = decltype(tc)::value;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        acc[e] += static_cast<int64_t>(static_cast<int32_t>(tp.x[T])) *
+                  static_cast<int32_t>(v[HE + e + (T - R) * C]);
+    });
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int64_t c = acc[e] > 32767 ? 32767 : (acc[e] < -32768 ? -32768 : acc[e]);
+      o[e] = static_cast<uint32_t>(c) & 0xFFFFu;
+    }
+  }
   return make_uint4(o[0] | (o[1] << 16), o[2] | (o[3] << 16), o[4] | (o[5] << 16),
                     o[6] | (o[7] << 16));
 }
@@ -522,7 +471,7 @@ __device__ __forceinline__ uint4 horizontal_s16(const int32_t *v_s, int tid, con
 // the binomial [1 4 6 4 1] (blur_and_downsample_neon.cpp:128-177).
 template <int C>
 __device__ __forceinline__ uint2 horizontal_blurdown(const uint32_t *vlo_s, const uint32_t *vhi_s,
-                                                     int tid, long out_elem0, int span_elem0) {
+                                                     long out_elem0, int span_elem0) {
   uint32_t o[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -541,7 +490,6 @@ __device__ __forceinline__ uint2 horizontal_blurdown(const uint32_t *vlo_s, cons
     }
     o[k] = (acc >> 8) & 0xFFu;
   }
-  (void)tid;
   return make_uint2(o[0] | (o[1] << 8) | (o[2] << 16) | (o[3] << 24),
                     o[4] | (o[5] << 8) | (o[6] << 16) | (o[7] << 24));
 }
@@ -552,7 +500,7 @@ __device__ __forceinline__ uint2 horizontal_blurdown(const uint32_t *vlo_s, cons
 // side, which overlap the neighbouring warps' interiors.  A warp therefore
 // needs no other warp's data and synchronises only with __syncwarp; the warps
 // of a CTA share the TMA ring through full/empty mbarrier pairs, and lane 0 of
-// warp 0 issues the copies between its own blocks of rows.
+// one warp issues the copies between its own blocks of rows.
 struct CtaShape {
   int warps;        // warps of the CTA
   int wi;           // interior chunks per warp
@@ -572,44 +520,40 @@ __host__ __device__ inline CtaShape cta_shape(int threads, int hc, int lbw) {
   return s;
 }
 
-template <int MODE>
-__host__ __device__ constexpr uint32_t vrow_bytes_per_lane() {
-  // lane form: lo + hi words (32 B); u16: 16 B; s32: 32 B.
-  return MODE == MODE_SEP_U16 ? 16u : 32u;
-}
-
-struct SmemLayout {
-  uint32_t ring_stage_bytes, span_area, edge_off, edge_warp_bytes, v_off, v_warp_bytes, bar_off,
-      total;
-};
-
 // Chunks per warp that can hang over the image's left/right edge and are
 // rebuilt in a per-warp edge area: at most HC on the left plus HC + 1 on the
 // right.
 __host__ __device__ constexpr int edge_slots(int hc) { return 2 * hc + 1; }
 
-// A ring stage holds stage_rows rows.  With TMA: the staged span laid out as
-// [box][row][box bytes] followed by two 256-byte-wide wrap areas
-// ([area][row][256 B]) that receive the far end of the row when a WRAP border
-// needs it; chunks hanging over the left/right edge are rebuilt in the edge
-// area.  Without TMA every lane owns a private 16-byte slot per row
-// ([warp][row][32 x 16 B]).
-template <int MODE>
-__host__ __device__ inline SmemLayout smem_layout(int threads, int hc, int lbw, int stage_rows,
-                                                  int stages) {
+constexpr uint32_t kBarBytes = 256;      // full[stages] + empty[stages], stages <= 16
+constexpr uint32_t kVRowBytes = 32 * 32;  // one V row of a warp: 32 lanes x 8 words
+
+// Shared memory of one CTA:
+//   [0, 256)     mbarriers
+//   ring         TMA: [box][ring row][box bytes]; plain loads: [ring row][warp][lane][16 B]
+//   wrap         (TMA with a WRAP border) [2][ring row][256 B]
+//   edge         (TMA) per warp [ring row][edge_slots][16 B]: chunks rebuilt by
+//                generic stores (never written by TMA, so no proxy fence)
+//   V            per warp [block_out_rows][kVRowBytes]
+struct SmemLayout {
+  uint32_t ring_off, ring_rows, wrap_off, edge_off, edge_warp_bytes, v_off, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int mode, int k, int threads, int hc, int lbw,
+                                                  int stage_rows, int stages, bool use_tma,
+                                                  bool wrap) {
   const CtaShape s = cta_shape(threads, hc, lbw);
   SmemLayout l;
-  const uint32_t tma_row = s.span_bytes + 512, own_row = s.warps * 32 * kChunk;
-  l.span_area = static_cast<uint32_t>(stage_rows) * s.span_bytes;
-  l.ring_stage_bytes = static_cast<uint32_t>(stage_rows) * (tma_row > own_row ? tma_row : own_row);
-  // Edge area: [warp][stage][row][edge_slots x 16 B], written only by generic
-  // stores (never by TMA), so it needs no proxy fence.
-  l.edge_off = l.ring_stage_bytes * stages;
-  l.edge_warp_bytes = static_cast<uint32_t>(stages) * stage_rows * edge_slots(hc) * kChunk;
+  l.ring_rows = static_cast<uint32_t>(stage_rows * stages);
+  l.ring_off = kBarBytes;
+  const uint32_t ring_bytes = use_tma ? l.ring_rows * static_cast<uint32_t>(s.span_bytes)
+                                      : l.ring_rows * s.warps * 32 * kChunk;
+  l.wrap_off = l.ring_off + ring_bytes;
+  const uint32_t wrap_bytes = (use_tma && wrap) ? 2 * l.ring_rows * 256 : 0;
+  l.edge_off = l.wrap_off + wrap_bytes;
+  l.edge_warp_bytes = use_tma ? l.ring_rows * edge_slots(hc) * kChunk : 0;
   l.v_off = l.edge_off + s.warps * l.edge_warp_bytes;
-  l.v_warp_bytes = 2 * 32 * vrow_bytes_per_lane<MODE>();  // double-buffered
-  l.bar_off = l.v_off + s.warps * l.v_warp_bytes;
-  l.total = l.bar_off + 16 * stages;  // full[stages] + empty[stages]
+  l.total = l.v_off + s.warps * block_out_rows(mode, k) * kVRowBytes;
   return l;
 }
 
@@ -626,25 +570,30 @@ struct TmaMaps {
 // One tile: strip `strip` x band `band` of job `j`.  `gstage` counts ring
 // stages used by this CTA so far (mbarrier phases continue across tiles).
 // stage_rows and stages are powers of two.
-template <int MODE, int K, int C>
+template <int MODE, int K, int C, bool NARROW>
 __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps, int strip,
                                          int band, uint8_t *smem, uint32_t &gstage,
                                          int *err_flag, bool &timed_out) {
   using G = Geo<MODE, K, C>;
-  using Row = typename RowOf<MODE, K>::type;
   constexpr int ES = G::ES;
   constexpr int HC = G::HC;
   constexpr int E = kChunk / ES;
+  constexpr int M = block_out_rows(MODE, K);
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int lbw = j.box_lbw;
   const CtaShape sh = cta_shape(blockDim.x, HC, lbw);
   const int rb = j.stage_rows, ns = j.stages;
   const int lrb = __ffs(rb) - 1, lns = __ffs(ns) - 1;
-  const SmemLayout L = smem_layout<MODE>(blockDim.x, HC, lbw, rb, ns);
-  uint8_t *ring = smem;
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+  const bool use_tma = j.use_tma != 0;
+  const SmemLayout L = smem_layout(MODE, K, blockDim.x, HC, lbw, rb, ns, use_tma,
+                                   j.border == BORDER_WRAP);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + ns;
+  uint8_t *const ring = smem + L.ring_off;
+  uint8_t *const wrap = smem + L.wrap_off;
+  const int ring_rows = static_cast<int>(L.ring_rows);
+  const uint32_t ring_mask = L.ring_rows - 1;
 
   const int oy0 = band * j.tile_rows;
   const int orows = min(j.tile_rows, j.out_height - oy0);
@@ -653,44 +602,43 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const long xs = static_cast<long>(strip) * sh.warps * sh.wi * kChunk - HC * kChunk;
   const long wc = static_cast<long>(j.width) * C;
   const long wcb = wc * ES;
-  const bool use_tma = j.use_tma != 0;
   const int nstages = (in_rows + rb - 1) >> lrb;
   // The producer is lane 0 of a warp whose chunks never hang over a strip's
   // left edge (warp 1 when the CTA has three or more warps): edge warps
   // already carry the cooperative border patching.
   const int pw = sh.warps >= 3 ? 1 : 0;
 
-  SpanGeo sg;
-  sg.xs = xs;
-  sg.span_end = xs + sh.span_bytes;
-  sg.wcb = wcb;
-  sg.lbw = lbw;
-  sg.rb = rb;
-  sg.span_area = static_cast<int>(L.span_area);
+  RingGeo rg;
+  rg.xs = xs;
+  rg.span_end = xs + sh.span_bytes;
+  rg.wcb = wcb;
+  rg.lbw = lbw;
+  rg.ring_rows = ring_rows;
   {
     // The wrap areas are filled only for a WRAP border on a strip that touches
     // exactly one side of the image (a strip spanning both sides already
     // holds the far end of the row).
-    const bool left = xs < 0, right = sg.span_end > wcb;
-    sg.wrap_left = j.border == BORDER_WRAP && left && !right;
-    sg.wrap_right = j.border == BORDER_WRAP && right && !left;
+    const bool left = xs < 0, right = rg.span_end > wcb;
+    rg.wrap_left = use_tma && j.border == BORDER_WRAP && left && !right;
+    rg.wrap_right = use_tma && j.border == BORDER_WRAP && right && !left;
     const long hb = static_cast<long>(G::HALO_ELEMS) * ES;
-    sg.wrapl_x = wcb - hb > 0 ? ((wcb - hb) & ~15L) : 0;
+    rg.wrapl_x = wcb - hb > 0 ? ((wcb - hb) & ~15L) : 0;
   }
 
-  // ======================= producer (lane 0 of warp 0) =======================
-  // fn(map, x in map units, destination, box width) for every box of a stage.
+  // ======================= producer (lane 0 of warp pw) ======================
+  // fn(map, x in map units, destination, box width) for every box of the
+  // rows starting at ring row `rr`.
   const int bw = 1 << lbw, unit_shift = lbw - 8;  // span map unit = 1 << unit_shift bytes
-  auto for_each_box = [&](uint8_t *base, bool single_row, auto &&fn) {
+  auto for_each_box = [&](int rr, bool single_row, auto &&fn) {
     for (int b = 0; b < sh.boxes; ++b) {
       const long x = xs + static_cast<long>(b) * bw;
       if (x < wcb && x + bw > 0)
-        fn(single_row ? maps.span_row : maps.span, x >> unit_shift, base + b * rb * bw,
-           static_cast<uint32_t>(bw));
+        fn(single_row ? maps.span_row : maps.span, x >> unit_shift,
+           ring + (b * ring_rows + rr) * bw, static_cast<uint32_t>(bw));
     }
-    uint8_t *wrap = base + L.span_area;
-    if (sg.wrap_left) fn(single_row ? maps.wrap_row : maps.wrap, sg.wrapl_x, wrap, 256u);
-    if (sg.wrap_right) fn(single_row ? maps.wrap_row : maps.wrap, 0L, wrap + rb * 256, 256u);
+    if (rg.wrap_left) fn(single_row ? maps.wrap_row : maps.wrap, rg.wrapl_x, wrap + rr * 256, 256u);
+    if (rg.wrap_right)
+      fn(single_row ? maps.wrap_row : maps.wrap, 0L, wrap + (ring_rows + rr) * 256, 256u);
   };
   // Copies stage s into its slot (the slot must be free).  Rows inside the
   // image arrive as stage_rows-high boxes; a stage that reaches outside gets
@@ -699,17 +647,17 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   auto issue_stage = [&](int s) {
     const uint32_t g = gstage + s;
     const int slot = static_cast<int>(g & (ns - 1));
-    uint8_t *base = ring + slot * L.ring_stage_bytes;
     uint64_t *bar = &full[slot];
     const int y = iy0 + s * rb;
+    const int rr0 = slot * rb;
     const bool rows_in = y >= 0 && y + rb <= j.height;
     uint32_t tx = 0;
     if (rows_in) {
-      for_each_box(base, false, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w * rb; });
+      for_each_box(rr0, false, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w * rb; });
     } else {
       for (int r = 0; r < rb; ++r)
         if (map_index(y + r, j.height, j.border) >= 0)
-          for_each_box(base, true, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w; });
+          for_each_box(rr0 + r, true, [&](const CUtensorMap *, long, uint8_t *, uint32_t w) { tx += w; });
     }
     if (tx == 0) {
       mbar_arrive(bar);
@@ -717,15 +665,15 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     }
     mbar_arrive_expect_tx(bar, tx);
     if (rows_in) {
-      for_each_box(base, false, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
+      for_each_box(rr0, false, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
         tma_load_2d(d, m, static_cast<int>(x), y, bar);
       });
     } else {
       for (int r = 0; r < rb; ++r) {
         const int my = map_index(y + r, j.height, j.border);
         if (my >= 0)
-          for_each_box(base, true, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t w) {
-            tma_load_2d(d + r * w, m, static_cast<int>(x), my, bar);
+          for_each_box(rr0 + r, true, [&](const CUtensorMap *m, long x, uint8_t *d, uint32_t) {
+            tma_load_2d(d, m, static_cast<int>(x), my, bar);
           });
       }
     }
@@ -774,13 +722,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const uint32_t bv_elem = ES == 1 ? (static_cast<uint32_t>(j.border_value) & 0xFFu)
                                    : (static_cast<uint32_t>(j.border_value) & 0xFFFFu);
   const uint32_t bv_word = ES == 1 ? bv_elem * 0x01010101u : bv_elem * 0x00010001u;
-  // Where lane `l` of this warp keeps its chunk of row 0 of a stage, and the
-  // distance between rows.
-  auto chunk_offset = [&](int l) {
-    return use_tma ? span_offset(sg, 0, (warp * sh.wi + l) * kChunk) : (warp * rb * 32 + l) * kChunk;
-  };
-  const int row_pitch = use_tma ? (1 << lbw) : 32 * kChunk;
-  const int chunk_off = chunk_offset(lane);
+  // Without TMA every lane owns a 16-byte slot per ring row.
+  const int own_pitch = sh.warps * 32 * kChunk;
+  auto own_slot = [&](int l) { return ring + (warp * 32 + l) * kChunk; };
   // Lanes whose chunk is not plain image data in every row: hanging over the
   // left/right edge, or (without TMA) not loadable with 16-byte loads.
   // (load_chunk_fast succeeds in every row when the chunk is 16-byte aligned
@@ -796,11 +740,22 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // With TMA, chunks rebuilt by the warp live in the edge area at compact slot
   // `edge_slot`; every other chunk is read where TMA put it.
   uint8_t *const edge_warp = smem + L.edge_off + warp * L.edge_warp_bytes;
+  const int edge_pitch = edge_slots(HC) * kChunk;
   const int edge_slot = __popc(coop_lanes & ((1u << lane) - 1u));
   const bool from_edge = use_tma && ((coop_lanes >> lane) & 1u);
-  const uint8_t *const lane_ring = from_edge ? edge_warp + edge_slot * kChunk : ring + chunk_off;
-  const int lane_stage_bytes = from_edge ? rb * edge_slots(HC) * kChunk : static_cast<int>(L.ring_stage_bytes);
-  const int lane_row_pitch = from_edge ? edge_slots(HC) * kChunk : row_pitch;
+  const uint8_t *lane_base;
+  uint32_t lane_pitch;
+  if (!use_tma) {
+    lane_base = own_slot(lane);
+    lane_pitch = static_cast<uint32_t>(own_pitch);
+  } else if (from_edge) {
+    lane_base = edge_warp + edge_slot * kChunk;
+    lane_pitch = static_cast<uint32_t>(edge_pitch);
+  } else {
+    const int o = cidx * kChunk;  // offset within the span
+    lane_base = ring + (o >> lbw) * ring_rows * bw + (o & (bw - 1));
+    lane_pitch = static_cast<uint32_t>(bw);
+  }
   // Rows of a CONSTANT border are substituted when read (TMA never fetched them).
   const bool const_rows = use_tma && j.border == BORDER_CONSTANT;
 
@@ -826,7 +781,6 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   auto prepare_stage = [&](int s) {
     const uint32_t g = gstage + s;
     const int slot = static_cast<int>(g & (ns - 1));
-    uint8_t *base = ring + slot * L.ring_stage_bytes;
     if (use_tma && !timed_out && !mbar_wait_bounded(&full[slot], (g >> lns) & 1u, kWaitLimitNs)) {
       timed_out = true;
       atomicOr(err_flag, 1);
@@ -836,7 +790,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
 #pragma unroll 1
       for (int r = 0; r < rows; ++r) {
         const int iy = iy0 + s * rb + r;
-        uint4 *dst = reinterpret_cast<uint4 *>(base + chunk_off + r * row_pitch);
+        uint4 *dst = reinterpret_cast<uint4 *>(own_slot(lane) + (slot * rb + r) * own_pitch);
         if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) {
           if (active) *dst = make_uint4(bv_word, bv_word, bv_word, bv_word);
         } else if (active && self_load_ok) {
@@ -852,14 +806,14 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     for (unsigned m = coop_lanes; m; m &= m - 1, ++k) {
       const int l = __ffs(m) - 1;
       const int x0 = static_cast<int>((xs + static_cast<long>(warp * sh.wi + l) * kChunk) / ES);
-      uint8_t *lbase = use_tma ? edge_warp + slot * rb * edge_slots(HC) * kChunk + k * kChunk
-                               : base + chunk_offset(l);
-      const int lpitch = use_tma ? edge_slots(HC) * kChunk : row_pitch;
+      uint8_t *lbase = use_tma ? edge_warp + k * kChunk : own_slot(l);
+      const int lpitch = use_tma ? edge_pitch : own_pitch;
 #pragma unroll 1
       for (int idx = lane; idx < rows * E; idx += 32) {
         const int r = idx / E, e = idx % E;
         const int iy = iy0 + s * rb + r;
         if (j.border == BORDER_CONSTANT && (iy < 0 || iy >= j.height)) continue;
+        const int rr = slot * rb + r;
         const int x = x0 + e;
         const bool inside = x >= 0 && x < static_cast<int>(wc);
         int me = x;
@@ -872,14 +826,14 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         if (me < 0) {
           v = bv_elem;
         } else if (use_tma) {
-          v = staged_byte(base, sg, r, static_cast<long>(me) * ES);
-          if (ES == 2) v |= staged_byte(base, sg, r, static_cast<long>(me) * ES + 1) << 8;
+          v = staged_byte(ring, wrap, rg, rr, static_cast<long>(me) * ES);
+          if (ES == 2) v |= staged_byte(ring, wrap, rg, rr, static_cast<long>(me) * ES + 1) << 8;
         } else {
           const uint8_t *grow =
               j.src + static_cast<int64_t>(map_index(iy, j.height, j.border)) * j.src_stride;
           v = ES == 1 ? __ldg(grow + me) : __ldg(reinterpret_cast<const uint16_t *>(grow) + me);
         }
-        uint8_t *dst = lbase + r * lpitch + e * ES;
+        uint8_t *dst = lbase + rr * lpitch + e * ES;
         dst[0] = static_cast<uint8_t>(v);
         if (ES == 2) dst[1] = static_cast<uint8_t>(v >> 8);
       }
@@ -893,125 +847,96 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     if (lane == 0) mbar_arrive(&empty[(gstage + s) & (ns - 1)]);
   };
 
-  uint32_t *vwarp = reinterpret_cast<uint32_t *>(smem + L.v_off + warp * L.v_warp_bytes);
-  constexpr uint32_t kVRowWords = 32 * vrow_bytes_per_lane<MODE>() / 4;
-  Row win[K];
-  int emitted = 0;
-  int stage_of_block = 0;  // stage of row qb
-  int row_of_block = 0;    // qb % rb
-
-  auto load_row = [&](int q, int u, Row &dst_row) {
-    // Row qb + u: stage and row within it from the block's base, no division.
-    const int r = row_of_block + u;
-    const int slot = static_cast<int>((gstage + stage_of_block + (r >> lrb)) & (ns - 1));
-    uint4 raw = *reinterpret_cast<const uint4 *>(lane_ring + slot * lane_stage_bytes +
-                                                 (r & (rb - 1)) * lane_row_pitch);
-    if (const_rows) {
-      const int iy = iy0 + q;
-      if (iy < 0 || iy >= j.height) raw = make_uint4(bv_word, bv_word, bv_word, bv_word);
-    }
-    unpack_row<MODE, K>(raw, dst_row);
-  };
-
-  // Hoisted per-tile values used by every emitted row.
+  uint32_t *const vwarp = reinterpret_cast<uint32_t *>(smem + L.v_off + warp * M * kVRowBytes);
   uint8_t *const dst_base = j.dst;
   const int64_t dst_stride = j.dst_stride;
   // Lanes outside the interior compute a duplicate of their nearest interior
   // neighbour's horizontal pass (never stored), so that no branch is needed.
   const int hlane = min(max(lane, HC), 31 - HC);
   const bool partial_store = stores && !full_store;
+  constexpr int NIN = block_in_rows(MODE, K);
 
-  auto emit = [&](auto rot_c, int q) {
-    constexpr int ROT = decltype(rot_c)::value;
-    uint32_t *vbuf = vwarp + (emitted & 1) * kVRowWords;
-    // ---- vertical pass -> the warp's shared row (every lane; lanes past the
-    // right halo hold stale data that no stored result reads)
-    if constexpr (ModeTraits<MODE>::LANES) {
-      uint32_t v[8];
-      vertical_lanes<MODE, K, ROT>(win, tp, v);
-      *reinterpret_cast<uint4 *>(vbuf + 4 * lane) = make_uint4(v[0], v[1], v[2], v[3]);
-      *reinterpret_cast<uint4 *>(vbuf + 128 + 4 * lane) = make_uint4(v[4], v[5], v[6], v[7]);
-    } else if constexpr (MODE == MODE_SEP_U16) {
-      uint32_t v[8];
-      vertical_u16<K, ROT>(win, tp, v);
-      *reinterpret_cast<uint4 *>(vbuf + 4 * lane) =
-          make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16),
-                     v[6] | (v[7] << 16));
-    } else {
-      int32_t v[8];
-      vertical_s16<K, ROT>(win, tp, v);
-      int32_t *vs = reinterpret_cast<int32_t *>(vbuf);
-      *reinterpret_cast<int4 *>(vs + 8 * lane) = make_int4(v[0], v[1], v[2], v[3]);
-      *reinterpret_cast<int4 *>(vs + 8 * lane + 4) = make_int4(v[4], v[5], v[6], v[7]);
-    }
-    __syncwarp();
-    // ---- horizontal pass + store
-    const int oy = MODE == MODE_BLURDOWN ? oy0 + (q - 4) / 2 : oy0 + q - (K - 1);
-    uint8_t *drow = dst_base + static_cast<int64_t>(oy) * dst_stride;
-    if constexpr (MODE == MODE_BLURDOWN) {
-      if (emits && active) {
-        const long ob = xb / 2;  // destination byte (= element) offset
-        const long owc = static_cast<long>(j.out_width) * C;
-        if (ob < owc) {
-          const uint2 r = horizontal_blurdown<C>(vbuf, vbuf + 128, lane, ob,
-                                                 static_cast<int>(xb - lane * kChunk));
-          if (ob + 8 <= owc && (reinterpret_cast<uintptr_t>(drow + ob) & 7) == 0) {
-            *reinterpret_cast<uint2 *>(drow + ob) = r;
-          } else {
-            const uint32_t w2[2] = {r.x, r.y};
-            for (int k = 0; k < 8 && ob + k < owc; ++k)
-              drow[ob + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
-          }
-        }
-      }
-    } else {
-      uint4 r;
-      if constexpr (ModeTraits<MODE>::LANES)
-        r = horizontal_lanes<MODE, K, C>(vbuf, vbuf + 128, hlane, tp);
-      else if constexpr (MODE == MODE_SEP_U16)
-        r = horizontal_u16<K, C>(vbuf, hlane, tp);
-      else
-        r = horizontal_s16<K, C>(reinterpret_cast<const int32_t *>(vbuf), hlane, tp);
-      if (full_store) st_v4(drow + xb, r);
-      if (partial_store) {
-        const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
-        for (int k = 0; k < kChunk && xb + k < wcb; ++k)
-          drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
-      }
-    }
-    ++emitted;
-  };
-
-  // ---- rows in blocks of K (window slot of every tap = compile-time index).
-  // Before a block, the stages of rows already consumed are released FIRST,
-  // then the stages the block's rows touch are readied (single call sites keep
-  // the rarely used border code out of the unrolled body).  A warp at block qb
-  // waits for stage (qb+K-1)/stage_rows, whose slot was last used by stage
-  // (qb+K-1)/stage_rows - stages; with stages >= (K-1)/stage_rows + 2 every
-  // warp has already released that stage, so the producer can always issue
-  // what the most advanced warp waits for, and a slower warp never waits for
-  // a faster one.
+  // ---- output rows in blocks of M.  Before a block, the stages holding only
+  // rows below the block are released FIRST, then the stages the block reads
+  // are readied.  A block reads at most floor((stage_rows - 1 + NIN - 1) /
+  // stage_rows) + 1 stages; with at least that many stages in the ring, the
+  // slot of every stage a warp waits for was released by all warps (each has
+  // released everything below its own block), so the producer can always
+  // issue what the most advanced warp waits for.
   int ready = 0, released = 0;
-  for (int qb = 0; qb < in_rows; qb += K) {
-    const int last_stage = (min(qb + K, in_rows) - 1) >> lrb;
-    for (; released < ready && ((released + 1) << lrb) <= qb; ++released) release_stage(released);
+  for (int ob = 0; ob < orows; ob += M) {
+    const int q0 = MODE == MODE_BLURDOWN ? 2 * ob : ob;
+    const int last_stage = (min(q0 + NIN, in_rows) - 1) >> lrb;
+    for (; released < ready && ((released + 1) << lrb) <= q0; ++released) release_stage(released);
     if (warp == pw) produce(last_stage);
     for (; ready <= last_stage; ++ready) prepare_stage(ready);
-    stage_of_block = qb >> lrb;
-    row_of_block = qb & (rb - 1);
-    static_for<0, K>([&](auto uc) {
-      constexpr int U = decltype(uc)::value;
-      const int q = qb + U;
-      if (q < in_rows) {
-        load_row(q, U, win[U]);
-        bool do_emit;
-        if constexpr (MODE == MODE_BLURDOWN)
-          do_emit = q >= 4 && ((q - 4) & 1) == 0;
-        else
-          do_emit = q >= K - 1;
-        if (do_emit) emit(std::integral_constant<int, (U + 1) % K>{}, q);
+    // Source rows of the block that lie in a CONSTANT border (above or below
+    // the image) read as the border value.
+    uint32_t cmask = 0;
+    if (const_rows) {
+      const int top = iy0 + q0;  // image row of the block's first source row
+      const int above = min(max(-top, 0), NIN);
+      const int inside_end = min(max(j.height - top, 0), NIN);
+      const uint32_t all = NIN >= 32 ? 0xFFFFFFFFu : ((1u << NIN) - 1u);
+      cmask = (((1u << above) - 1u) | (all & ~((1u << inside_end) - 1u))) & all;
+    }
+    // Rows past the band's end (last block) read stale ring rows; they only
+    // feed output rows that are not stored.
+    uint32_t v[M][8];
+    vertical_block<MODE, K, NARROW>(lane_base, lane_pitch,
+                                    gstage * static_cast<uint32_t>(rb) + static_cast<uint32_t>(q0),
+                                    ring_mask, cmask, bv_word, tp, v);
+    static_for<0, M>([&](auto mc) {
+      constexpr int Mi = decltype(mc)::value;
+      uint32_t *vb = vwarp + Mi * (kVRowBytes / 4);
+      if constexpr (ModeTraits<MODE>::LANES) {
+        *reinterpret_cast<uint4 *>(vb + 4 * lane) = make_uint4(v[Mi][0], v[Mi][1], v[Mi][2], v[Mi][3]);
+        *reinterpret_cast<uint4 *>(vb + 128 + 4 * lane) =
+            make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
+      } else {
+        *reinterpret_cast<uint4 *>(vb + 8 * lane) = make_uint4(v[Mi][0], v[Mi][1], v[Mi][2], v[Mi][3]);
+        *reinterpret_cast<uint4 *>(vb + 8 * lane + 4) =
+            make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
       }
     });
+    __syncwarp();
+    // ---- horizontal pass + store, one output row at a time
+    const int mcount = min(M, orows - ob);
+#pragma unroll 1
+    for (int m = 0; m < mcount; ++m) {
+      const uint32_t *vb = vwarp + m * (kVRowBytes / 4);
+      uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + m) * dst_stride;
+      if constexpr (MODE == MODE_BLURDOWN) {
+        if (emits && active) {
+          const long ob8 = xb / 2;  // destination byte (= element) offset
+          const long owc = static_cast<long>(j.out_width) * C;
+          if (ob8 < owc) {
+            const uint2 r = horizontal_blurdown<C>(vb, vb + 128, ob8,
+                                                   static_cast<int>(xb - lane * kChunk));
+            if (ob8 + 8 <= owc && (reinterpret_cast<uintptr_t>(drow + ob8) & 7) == 0) {
+              *reinterpret_cast<uint2 *>(drow + ob8) = r;
+            } else {
+              const uint32_t w2[2] = {r.x, r.y};
+              for (int k = 0; k < 8 && ob8 + k < owc; ++k)
+                drow[ob8 + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
+            }
+          }
+        }
+      } else {
+        uint4 r;
+        if constexpr (ModeTraits<MODE>::LANES)
+          r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
+        else
+          r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
+        if (full_store) st_v4(drow + xb, r);
+        if (partial_store) {
+          const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
+          for (int k = 0; k < kChunk && xb + k < wcb; ++k)
+            drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
+        }
+      }
+    }
+    __syncwarp();
   }
   for (; released < nstages; ++released) release_stage(released);
   if (use_tma && timed_out && warp == pw && lane == 0) {
@@ -1028,17 +953,15 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
 // ---------------------------------------------------------------------------
 // Launch: a grid of up to (resident CTAs per SM x SMs) CTAs that walk the
 // job's tiles (strip, band) in row-major band order; threads = 32 * warps.
-template <int MODE, int K, int C>
-__global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4)) sepfused_kernel(const __grid_constant__ FilterJob job,
-                                                          int *err_flag) {
+template <int MODE, int K, int C, bool NARROW>
+__global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
+    sepfused_kernel(const __grid_constant__ FilterJob job, int *err_flag) {
   extern __shared__ __align__(128) uint8_t smem[];
-  constexpr int HC = Geo<MODE, K, C>::HC;
-  const SmemLayout L = smem_layout<MODE>(blockDim.x, HC, job.box_lbw, job.stage_rows, job.stages);
   if (job.use_tma) {
     if (threadIdx.x == 0) {
       prefetch_tensormap(&job.tmap);
       prefetch_tensormap(&job.tmap_row);
-      uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+      uint64_t *full = reinterpret_cast<uint64_t *>(smem);
       const int warps = blockDim.x / 32;
       for (int s = 0; s < job.stages; ++s) {
         mbar_init(&full[s], 1);
@@ -1053,8 +976,8 @@ __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4)) sepfused_kernel(const 
   const TmaMaps maps{&job.tmap, &job.tmap_row, &job.tmap_wrap, &job.tmap_wrap_row};
   const int tiles = job.strips * job.row_tiles;
   for (int t = blockIdx.x; t < tiles; t += gridDim.x)
-    run_tile<MODE, K, C>(job, maps, t % job.strips, t / job.strips, smem, gstage, err_flag,
-                         timed_out);
+    run_tile<MODE, K, C, NARROW>(job, maps, t % job.strips, t / job.strips, smem, gstage,
+                                 err_flag, timed_out);
 }
 
 }  // namespace kcv
