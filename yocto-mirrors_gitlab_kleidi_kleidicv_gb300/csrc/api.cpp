@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <numeric>
 #include <mutex>
 
 #include "host.h"
@@ -287,12 +288,14 @@ TileShape tile_shape_for(const FilterJob &j, int sm_count) {
   return t;
 }
 
-// Ring depth rule: a block of output rows reads block_in_rows consecutive
-// source rows, which touch at most floor((stage_rows - 1 + in_rows - 1) /
-// stage_rows) + 1 stages; the ring holds at least that many stages, so a
-// consumer warp never waits for a stage that cannot be issued until a warp
-// behind it releases one.  Both counts are powers of two and the ring has at
-// most 16 stages (the mbarrier area), so large kernels get taller stages.
+// Ring depth rule.  A block of output rows reads block_in_rows consecutive
+// source rows starting at a multiple of the block's row step; `need` is the
+// most stages such a window can touch.  The ring holds need + 2 stages: the
+// block's own plus two stages of copies in flight ahead of it.  With at least
+// `need` stages a consumer warp never waits for a stage that cannot be issued
+// until a warp behind it releases one.  stage_rows is a power of two; the
+// ring has at most 16 stages (the mbarrier area), so large kernels get taller
+// stages.
 static void fix_ring(FilterJob &j) {
   auto pow2 = [](int v) {
     int p = 1;
@@ -300,11 +303,14 @@ static void fix_ring(FilterJob &j) {
     return p;
   };
   const int in_rows = block_in_rows(j.mode, j.ksize);
+  const int step = (j.mode == MODE_BLURDOWN ? 2 : 1) * block_out_rows(j.mode, j.ksize);
   int rb = std::max(1, std::min(pow2(j.stage_rows), 64));
   int ns = 0;
   for (;; rb <<= 1) {
-    const int need = (rb - 1 + in_rows - 1) / rb + 1;
-    ns = pow2(std::max({2, j.stages, need}));
+    const int g = std::gcd(step, rb);
+    int need = 1;
+    for (int o = 0; o < rb; o += g) need = std::max(need, (o + in_rows - 1) / rb + 1);
+    ns = std::max(j.stages, need + 2);
     if (ns <= 16 || rb >= 64) break;
   }
   j.stage_rows = rb;

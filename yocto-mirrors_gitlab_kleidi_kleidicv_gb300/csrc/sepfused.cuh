@@ -253,15 +253,13 @@ __device__ __forceinline__ uint32_t vfinish(uint32_t acc) {
 }
 
 // Vertical pass of one block: block_out_rows output rows from
-// block_in_rows consecutive ring rows starting at ring row rr0.  Each source
+// block_in_rows consecutive ring rows starting at ring row rr0 (modulo
+// ring_rows).  Each source
 // row is read from shared memory and unpacked once, then added into every
 // output row it belongs to (taps outer, lanes inner: independent chains).
-// Rows whose bit is set in `cmask` lie in a CONSTANT border and read as the
-// border value.
 template <int MODE, int K, bool NARROW>
 __device__ __forceinline__ void vertical_block(const uint8_t *lane_base, uint32_t pitch,
-                                               uint32_t rr0, uint32_t ring_mask, uint32_t cmask,
-                                               uint32_t bv_word, const Taps &tp,
+                                               uint32_t rr0, uint32_t ring_rows, const Taps &tp,
                                                uint32_t (&v)[block_out_rows(MODE, K)][8]) {
   constexpr int M = block_out_rows(MODE, K);
   constexpr int NIN = block_in_rows(MODE, K);
@@ -274,8 +272,9 @@ __device__ __forceinline__ void vertical_block(const uint8_t *lane_base, uint32_
   });
   static_for<0, NIN>([&](auto ic) {
     constexpr int I = decltype(ic)::value;
-    uint4 raw = *reinterpret_cast<const uint4 *>(lane_base + ((rr0 + I) & ring_mask) * pitch);
-    if (cmask & (1u << I)) raw = make_uint4(bv_word, bv_word, bv_word, bv_word);
+    uint32_t rr = rr0 + I;  // rr0 < ring_rows and I < ring_rows: one wrap at most
+    if (rr >= ring_rows) rr -= ring_rows;
+    const uint4 raw = *reinterpret_cast<const uint4 *>(lane_base + rr * pitch);
     uint32_t x[8];
     unpack_chunk<MODE>(raw, x);
     static_for<0, M>([&](auto mc) {
@@ -529,12 +528,12 @@ constexpr uint32_t kBarBytes = 256;      // full[stages] + empty[stages], stages
 constexpr uint32_t kVRowBytes = 32 * 32;  // one V row of a warp: 32 lanes x 8 words
 
 // Shared memory of one CTA:
-//   [0, 256)     mbarriers
+//   [0, 256)     mbarriers full[stages], empty[stages] (stages <= 16)
 //   ring         TMA: [box][ring row][box bytes]; plain loads: [ring row][warp][lane][16 B]
 //   wrap         (TMA with a WRAP border) [2][ring row][256 B]
 //   edge         (TMA) per warp [ring row][edge_slots][16 B]: chunks rebuilt by
 //                generic stores (never written by TMA, so no proxy fence)
-//   V            per warp [block_out_rows][kVRowBytes]
+//   V            per warp [2][kVRowBytes] (double-buffered vertical row)
 struct SmemLayout {
   uint32_t ring_off, ring_rows, wrap_off, edge_off, edge_warp_bytes, v_off, total;
 };
@@ -553,7 +552,7 @@ __host__ __device__ inline SmemLayout smem_layout(int mode, int k, int threads, 
   l.edge_off = l.wrap_off + wrap_bytes;
   l.edge_warp_bytes = use_tma ? l.ring_rows * edge_slots(hc) * kChunk : 0;
   l.v_off = l.edge_off + s.warps * l.edge_warp_bytes;
-  l.total = l.v_off + s.warps * block_out_rows(mode, k) * kVRowBytes;
+  l.total = l.v_off + s.warps * 2 * kVRowBytes;
   return l;
 }
 
@@ -584,7 +583,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const int lbw = j.box_lbw;
   const CtaShape sh = cta_shape(blockDim.x, HC, lbw);
   const int rb = j.stage_rows, ns = j.stages;
-  const int lrb = __ffs(rb) - 1, lns = __ffs(ns) - 1;
+  const int lrb = __ffs(rb) - 1;
   const bool use_tma = j.use_tma != 0;
   const SmemLayout L = smem_layout(MODE, K, blockDim.x, HC, lbw, rb, ns, use_tma,
                                    j.border == BORDER_WRAP);
@@ -593,7 +592,20 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   uint8_t *const ring = smem + L.ring_off;
   uint8_t *const wrap = smem + L.wrap_off;
   const int ring_rows = static_cast<int>(L.ring_rows);
-  const uint32_t ring_mask = L.ring_rows - 1;
+  // Ring position of the tile's first stage: slot (gstage mod stages) and
+  // use count (gstage / stages, whose parity is the mbarrier phase).
+  const int base_slot = static_cast<int>(gstage % static_cast<uint32_t>(ns));
+  const uint32_t base_use = gstage / static_cast<uint32_t>(ns);
+  struct RingPos {
+    int slot;
+    uint32_t use;
+  };
+  auto advance = [&](RingPos &p) {
+    if (++p.slot == ns) {
+      p.slot = 0;
+      ++p.use;
+    }
+  };
 
   const int oy0 = band * j.tile_rows;
   const int orows = min(j.tile_rows, j.out_height - oy0);
@@ -644,9 +656,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // image arrive as stage_rows-high boxes; a stage that reaches outside gets
   // one single-row box per row of its border-mapped source row instead (none
   // for a CONSTANT border).
-  auto issue_stage = [&](int s) {
-    const uint32_t g = gstage + s;
-    const int slot = static_cast<int>(g & (ns - 1));
+  auto issue_stage = [&](int s, int slot) {
     uint64_t *bar = &full[slot];
     const int y = iy0 + s * rb;
     const int rr0 = slot * rb;
@@ -682,12 +692,12 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // `last_needed` (waiting, with a time limit, for its slot to be released),
   // then as many further stages as have free slots.
   int issued = 0;
+  RingPos ppos{base_slot, base_use};
   auto produce = [&](int last_needed) {
     if (use_tma && lane == 0) {
       while (issued < nstages && !timed_out) {
-        const uint32_t g = gstage + issued;
-        const int slot = static_cast<int>(g & (ns - 1));
-        const uint32_t use = g >> lns;
+        const int slot = ppos.slot;
+        const uint32_t use = ppos.use;
         if (use > 0) {
           if (issued <= last_needed) {
             if (!mbar_wait_bounded(&empty[slot], (use - 1) & 1u, kWaitLimitNs)) {
@@ -699,8 +709,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
             break;
           }
         }
-        issue_stage(issued);
+        issue_stage(issued, slot);
         ++issued;
+        advance(ppos);
       }
     }
     __syncwarp();
@@ -756,8 +767,6 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     lane_base = ring + (o >> lbw) * ring_rows * bw + (o & (bw - 1));
     lane_pitch = static_cast<uint32_t>(bw);
   }
-  // Rows of a CONSTANT border are substituted when read (TMA never fetched them).
-  const bool const_rows = use_tma && j.border == BORDER_CONSTANT;
 
   Taps tp;
   if constexpr (MODE == MODE_SIGMA) {
@@ -778,10 +787,12 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // elements come from the staged row (or, without TMA, every element from
   // global memory).  Lanes that share a chunk with a neighbouring warp write
   // identical bytes.
+  RingPos rpos{base_slot, base_use}, lpos{base_slot, base_use};
   auto prepare_stage = [&](int s) {
-    const uint32_t g = gstage + s;
-    const int slot = static_cast<int>(g & (ns - 1));
-    if (use_tma && !timed_out && !mbar_wait_bounded(&full[slot], (g >> lns) & 1u, kWaitLimitNs)) {
+    const int slot = rpos.slot;
+    const uint32_t phase = rpos.use & 1u;
+    advance(rpos);
+    if (use_tma && !timed_out && !mbar_wait_bounded(&full[slot], phase, kWaitLimitNs)) {
       timed_out = true;
       atomicOr(err_flag, 1);
     }
@@ -800,6 +811,19 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
                           xb, wcb, v);
           *dst = v;
         }
+      }
+    }
+    // TMA never fetches rows of a CONSTANT border: every lane fills its own
+    // chunk of them (lanes sharing a chunk write the same bytes), and fences
+    // those generic writes against the TMA copy that will reuse the slot.
+    if (use_tma && j.border == BORDER_CONSTANT) {
+      const int y0 = iy0 + s * rb;
+      if (y0 < 0 || y0 + rows > j.height) {
+        for (int r = 0; r < rows; ++r)
+          if (y0 + r < 0 || y0 + r >= j.height)
+            *reinterpret_cast<uint4 *>(const_cast<uint8_t *>(lane_base) + (slot * rb + r) * lane_pitch) =
+                make_uint4(bv_word, bv_word, bv_word, bv_word);
+        fence_proxy_async_smem();
       }
     }
     int k = 0;
@@ -841,13 +865,15 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     __syncwarp();
   };
   // Hands stage s back to the producer once every lane of the warp has read it.
-  auto release_stage = [&](int s) {
+  auto release_stage = [&]() {
     if (!use_tma) return;
+    const int slot = lpos.slot;
+    advance(lpos);
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[(gstage + s) & (ns - 1)]);
+    if (lane == 0) mbar_arrive(&empty[slot]);
   };
 
-  uint32_t *const vwarp = reinterpret_cast<uint32_t *>(smem + L.v_off + warp * M * kVRowBytes);
+  uint32_t *const vwarp = reinterpret_cast<uint32_t *>(smem + L.v_off + warp * 2 * kVRowBytes);
   uint8_t *const dst_base = j.dst;
   const int64_t dst_stride = j.dst_stride;
   // Lanes outside the interior compute a duplicate of their nearest interior
@@ -864,31 +890,28 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // released everything below its own block), so the producer can always
   // issue what the most advanced warp waits for.
   int ready = 0, released = 0;
+  int rq = base_slot * rb;  // ring row of the block's first source row
   for (int ob = 0; ob < orows; ob += M) {
     const int q0 = MODE == MODE_BLURDOWN ? 2 * ob : ob;
     const int last_stage = (min(q0 + NIN, in_rows) - 1) >> lrb;
-    for (; released < ready && ((released + 1) << lrb) <= q0; ++released) release_stage(released);
+    for (; released < ready && ((released + 1) << lrb) <= q0; ++released) release_stage();
     if (warp == pw) produce(last_stage);
     for (; ready <= last_stage; ++ready) prepare_stage(ready);
-    // Source rows of the block that lie in a CONSTANT border (above or below
-    // the image) read as the border value.
-    uint32_t cmask = 0;
-    if (const_rows) {
-      const int top = iy0 + q0;  // image row of the block's first source row
-      const int above = min(max(-top, 0), NIN);
-      const int inside_end = min(max(j.height - top, 0), NIN);
-      const uint32_t all = NIN >= 32 ? 0xFFFFFFFFu : ((1u << NIN) - 1u);
-      cmask = (((1u << above) - 1u) | (all & ~((1u << inside_end) - 1u))) & all;
-    }
     // Rows past the band's end (last block) read stale ring rows; they only
     // feed output rows that are not stored.
     uint32_t v[M][8];
-    vertical_block<MODE, K, NARROW>(lane_base, lane_pitch,
-                                    gstage * static_cast<uint32_t>(rb) + static_cast<uint32_t>(q0),
-                                    ring_mask, cmask, bv_word, tp, v);
+    vertical_block<MODE, K, NARROW>(lane_base, lane_pitch, static_cast<uint32_t>(rq),
+                                    static_cast<uint32_t>(ring_rows), tp, v);
+    rq += MODE == MODE_BLURDOWN ? 2 * M : M;
+    if (rq >= ring_rows) rq -= ring_rows;
+    // ---- horizontal pass + store, one output row at a time through the
+    // warp's two V rows: write row m, __syncwarp, read it.  Row m + 2 reuses
+    // the buffer only after the __syncwarp of row m + 1, when every lane has
+    // finished reading row m.
+    const int mcount = min(M, orows - ob);
     static_for<0, M>([&](auto mc) {
       constexpr int Mi = decltype(mc)::value;
-      uint32_t *vb = vwarp + Mi * (kVRowBytes / 4);
+      uint32_t *vb = vwarp + (Mi & 1) * (kVRowBytes / 4);
       if constexpr (ModeTraits<MODE>::LANES) {
         *reinterpret_cast<uint4 *>(vb + 4 * lane) = make_uint4(v[Mi][0], v[Mi][1], v[Mi][2], v[Mi][3]);
         *reinterpret_cast<uint4 *>(vb + 128 + 4 * lane) =
@@ -898,54 +921,47 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         *reinterpret_cast<uint4 *>(vb + 8 * lane + 4) =
             make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
       }
-    });
-    __syncwarp();
-    // ---- horizontal pass + store, one output row at a time
-    const int mcount = min(M, orows - ob);
-#pragma unroll 1
-    for (int m = 0; m < mcount; ++m) {
-      const uint32_t *vb = vwarp + m * (kVRowBytes / 4);
-      uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + m) * dst_stride;
-      if constexpr (MODE == MODE_BLURDOWN) {
-        if (emits && active) {
-          const long ob8 = xb / 2;  // destination byte (= element) offset
-          const long owc = static_cast<long>(j.out_width) * C;
-          if (ob8 < owc) {
-            const uint2 r = horizontal_blurdown<C>(vb, vb + 128, ob8,
-                                                   static_cast<int>(xb - lane * kChunk));
-            if (ob8 + 8 <= owc && (reinterpret_cast<uintptr_t>(drow + ob8) & 7) == 0) {
-              *reinterpret_cast<uint2 *>(drow + ob8) = r;
-            } else {
-              const uint32_t w2[2] = {r.x, r.y};
-              for (int k = 0; k < 8 && ob8 + k < owc; ++k)
-                drow[ob8 + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
+      __syncwarp();
+      if (Mi < mcount) {
+        uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + Mi) * dst_stride;
+        if constexpr (MODE == MODE_BLURDOWN) {
+          if (emits && active) {
+            const long ob8 = xb / 2;  // destination byte (= element) offset
+            const long owc = static_cast<long>(j.out_width) * C;
+            if (ob8 < owc) {
+              const uint2 r = horizontal_blurdown<C>(vb, vb + 128, ob8,
+                                                     static_cast<int>(xb - lane * kChunk));
+              if (ob8 + 8 <= owc && (reinterpret_cast<uintptr_t>(drow + ob8) & 7) == 0) {
+                *reinterpret_cast<uint2 *>(drow + ob8) = r;
+              } else {
+                const uint32_t w2[2] = {r.x, r.y};
+                for (int k = 0; k < 8 && ob8 + k < owc; ++k)
+                  drow[ob8 + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
+              }
             }
           }
-        }
-      } else {
-        uint4 r;
-        if constexpr (ModeTraits<MODE>::LANES)
-          r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
-        else
-          r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
-        if (full_store) st_v4(drow + xb, r);
-        if (partial_store) {
-          const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
-          for (int k = 0; k < kChunk && xb + k < wcb; ++k)
-            drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
+        } else {
+          uint4 r;
+          if constexpr (ModeTraits<MODE>::LANES)
+            r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
+          else
+            r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
+          if (full_store) *reinterpret_cast<uint4 *>(drow + xb) = r;
+          if (partial_store) {
+            const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
+            for (int k = 0; k < kChunk && xb + k < wcb; ++k)
+              drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
+          }
         }
       }
-    }
-    __syncwarp();
+    });
   }
-  for (; released < nstages; ++released) release_stage(released);
+  for (; released < nstages; ++released) release_stage();
   if (use_tma && timed_out && warp == pw && lane == 0) {
     // Give copies already issued a bounded time to land before the CTA's
     // shared memory can be reused.
-    for (int s2 = 0; s2 < issued; ++s2) {
-      const uint32_t g = gstage + s2;
-      mbar_wait_bounded(&full[g & (ns - 1)], (g >> lns) & 1u, kWaitLimitNs);
-    }
+    RingPos d{base_slot, base_use};
+    for (int s2 = 0; s2 < issued; ++s2, advance(d)) mbar_wait_bounded(&full[d.slot], d.use & 1u, kWaitLimitNs);
   }
   gstage += nstages;
 }
