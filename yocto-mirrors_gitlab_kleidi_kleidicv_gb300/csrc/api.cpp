@@ -339,18 +339,28 @@ void apply_tile_shape(FilterJob &j, const TileShape &t) {
   j.row_tiles = j.tile_rows > 0 ? (j.out_height + j.tile_rows - 1) / j.tile_rows : 0;
 }
 
-// Tile rows when the tile shape left them open: one tile per resident CTA of
-// a single wave (persistent CTAs walk the tiles), at least 8 rows per tile.
+// Bands when the tile shape left them open.  The resident CTAs of one wave
+// (occupancy x SMs) each take one tile, and every SM should get the same
+// work: the bands are whole blocks of output rows high, tile_rows or
+// tile_rows + block_out_rows, so that strips x bands fills the wave exactly
+// (a persistent CTA walks further tiles when there are more).
 void finish_plan(FilterJob &j, int sm_count) {
+  const int m = block_out_rows(j.mode, j.ksize);
+  j.big_bands = 0;
   if (j.tile_rows <= 0) {
     const int occ = std::max(1, fused_blocks_per_sm(j));
     const long target = static_cast<long>(occ) * std::max(sm_count, 1);
     const long bands = std::max(1L, target / std::max<long>(j.strips, 1));
-    int rows = static_cast<int>((j.out_height + bands - 1) / bands);
-    // Whole blocks of output rows per tile.
-    const int m = block_out_rows(j.mode, j.ksize);
-    rows = (rows + m - 1) / m * m;
-    j.tile_rows = std::max(8, std::min(rows, 1 << 20));
+    const long q = m * (j.out_height / (bands * m));
+    if (q == 0) {
+      j.tile_rows = m;
+      j.row_tiles = (j.out_height + m - 1) / m;
+    } else {
+      j.tile_rows = static_cast<int32_t>(q);
+      j.row_tiles = static_cast<int32_t>(bands);
+      j.big_bands = static_cast<int32_t>((j.out_height - bands * q) / m);
+    }
+    return;
   }
   j.row_tiles = (j.out_height + j.tile_rows - 1) / j.tile_rows;
 }

@@ -85,6 +85,9 @@ struct FilterJob {
   int32_t halo_chunks;
   int32_t strips;
   int32_t row_tiles;
+  // Bands 0 .. big_bands-1 are tile_rows + block_out_rows rows high, the
+  // others tile_rows; the last band ends at out_height.
+  int32_t big_bands;
   int32_t strip_out_bytes;  // destination bytes produced per strip
   int32_t box_lbw;          // log2 of the span box width in bytes (8 or 11)
 };

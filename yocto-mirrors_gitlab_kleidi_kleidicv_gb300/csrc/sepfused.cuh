@@ -607,8 +607,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     }
   };
 
-  const int oy0 = band * j.tile_rows;
-  const int orows = min(j.tile_rows, j.out_height - oy0);
+  const int oy0 = band * j.tile_rows + M * min(band, j.big_bands);
+  const int orows = band == j.row_tiles - 1 ? j.out_height - oy0
+                                            : j.tile_rows + (band < j.big_bands ? M : 0);
   const int iy0 = MODE == MODE_BLURDOWN ? 2 * oy0 - 2 : oy0 - G::R;
   const int in_rows = MODE == MODE_BLURDOWN ? 2 * orows + 3 : orows + K - 1;
   const long xs = static_cast<long>(strip) * sh.warps * sh.wi * kChunk - HC * kChunk;
