@@ -250,6 +250,66 @@ def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst
                                                ctypes.cast(ds, ctypes.c_void_p), border_type, _h(ctx))
 
 
+# --- batched execution -----------------------------------------------------
+
+def make_request(op, src, src_stride, dst, dst_stride, width, height, channels, kernel_width=0,
+                 kernel_height=0, sigma_x=0.0, sigma_y=0.0, kernel_x=None, kernel_y=None,
+                 border_type=REPLICATE, border_value=0, allow_extensions=False):
+    """kleidicv_gpu_request_t for one filter call (device pointers, byte strides)."""
+    r = Request()
+    r.op, r.src, r.src_stride, r.dst, r.dst_stride = op, src, src_stride, dst, dst_stride
+    r.width, r.height, r.channels = width, height, channels
+    r.kernel_width, r.kernel_height, r.sigma_x, r.sigma_y = kernel_width, kernel_height, sigma_x, sigma_y
+    for i, v in enumerate(kernel_x or [0] * 5):
+        r.kernel_x[i] = int(v)
+    for i, v in enumerate(kernel_y or [0] * 5):
+        r.kernel_y[i] = int(v)
+    r.border_type, r.border_value, r.allow_extensions = border_type, int(border_value), int(allow_extensions)
+    return r
+
+
+class BatchPlan:
+    """kleidicv_gpu_batch_plan_t: validated requests, tile work-lists, optional CUDA graph."""
+
+    def __init__(self, requests, ctx=None):
+        n = len(requests)
+        self._reqs = (Request * max(n, 1))(*requests)
+        self._statuses = (_i * max(n, 1))()
+        h = ctypes.c_void_p()
+        err = lib().kleidicv_gpu_batch_plan_create(self._reqs, n, self._statuses, ctypes.byref(h), _h(ctx))
+        if err != OK:
+            raise RuntimeError(f"kleidicv_gpu_batch_plan_create failed: {ERROR_NAMES.get(err, err)}")
+        self.handle = h
+        self.statuses = [int(self._statuses[i]) for i in range(n)]
+        self.ctx = ctx
+
+    def tile_count(self) -> int:
+        return lib().kleidicv_gpu_batch_plan_tile_count(self.handle)
+
+    def launch(self, use_graph=True) -> int:
+        return lib().kleidicv_gpu_batch_plan_launch(self.handle, int(use_graph), _h(self.ctx))
+
+    def close(self):
+        if self.handle:
+            lib().kleidicv_gpu_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_submit(requests, ctx=None):
+    """One-shot batch: returns (error, per-request statuses)."""
+    n = len(requests)
+    reqs = (Request * max(n, 1))(*requests)
+    st = (_i * max(n, 1))()
+    err = lib().kleidicv_gpu_batch_submit(reqs, n, st, _h(ctx))
+    return err, [int(st[i]) for i in range(n)]
+
+
 # --- torch helpers ---------------------------------------------------------
 
 def ptr(t):

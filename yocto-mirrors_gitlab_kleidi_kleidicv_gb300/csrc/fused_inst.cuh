@@ -4,14 +4,31 @@
 #include <algorithm>
 
 #include "launch.h"
-#include "sepfused.cuh"
+#include "batch_kernel.cuh"
 
 namespace kcv {
 
-// err_flag == nullptr: only report the occupancy in *blocks_per_sm.
+// Plain launch of `job` (batch == nullptr) or of the batched kernel of the
+// same instantiation over batch->tiles.  With blocks_per_sm set, only reports
+// the occupancy.
 template <int MODE, int K, int C, bool NARROW>
 cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
-                       int *blocks_per_sm = nullptr) {
+                       int *blocks_per_sm, const BatchLaunch *batch) {
+  if (batch) {
+    auto kern = batch_kernel<MODE, K, C, NARROW>;
+    static bool battr_set = false;  // per instantiation
+    if (!battr_set) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           200 * 1024);
+      if (e != cudaSuccess) return e;
+      battr_set = true;
+    }
+    if (blocks_per_sm)
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, 128, batch->smem);
+    kern<<<static_cast<unsigned>(batch->grid), 128, batch->smem, stream>>>(
+        batch->jobs, batch->tiles, batch->ntiles, batch->next_tile, err_flag);
+    return cudaGetLastError();
+  }
   const SmemLayout L = smem_layout(MODE, K, job.threads, job.halo_chunks, job.box_lbw,
                                    job.stage_rows, job.stages, job.use_tma != 0,
                                    job.border == BORDER_WRAP);
@@ -41,12 +58,12 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
 
 template <int MODE, int K, bool NARROW>
 bool dispatch_channels_n(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
-                         int *blocks_per_sm) {
+                         int *blocks_per_sm, const BatchLaunch *b) {
   switch (job.channels) {
-    case 1: *out = launch_one<MODE, K, 1, NARROW>(job, err, s, blocks_per_sm); return true;
-    case 2: *out = launch_one<MODE, K, 2, NARROW>(job, err, s, blocks_per_sm); return true;
-    case 3: *out = launch_one<MODE, K, 3, NARROW>(job, err, s, blocks_per_sm); return true;
-    case 4: *out = launch_one<MODE, K, 4, NARROW>(job, err, s, blocks_per_sm); return true;
+    case 1: *out = launch_one<MODE, K, 1, NARROW>(job, err, s, blocks_per_sm, b); return true;
+    case 2: *out = launch_one<MODE, K, 2, NARROW>(job, err, s, blocks_per_sm, b); return true;
+    case 3: *out = launch_one<MODE, K, 3, NARROW>(job, err, s, blocks_per_sm, b); return true;
+    case 4: *out = launch_one<MODE, K, 4, NARROW>(job, err, s, blocks_per_sm, b); return true;
   }
   return false;
 }
@@ -55,11 +72,11 @@ bool dispatch_channels_n(const FilterJob &job, int *err, cudaStream_t s, cudaErr
 // and blur-and-downsample arithmetic is narrow by construction.
 template <int MODE, int K>
 bool dispatch_channels(const FilterJob &job, int *err, cudaStream_t s, cudaError_t *out,
-                       int *blocks_per_sm = nullptr) {
+                       int *blocks_per_sm, const BatchLaunch *b) {
   if constexpr (MODE == MODE_SEP_U8 || MODE == MODE_SEP_U16 || MODE == MODE_SEP_S16) {
-    if (job.narrow) return dispatch_channels_n<MODE, K, true>(job, err, s, out, blocks_per_sm);
+    if (job.narrow) return dispatch_channels_n<MODE, K, true>(job, err, s, out, blocks_per_sm, b);
   }
-  return dispatch_channels_n<MODE, K, false>(job, err, s, out, blocks_per_sm);
+  return dispatch_channels_n<MODE, K, false>(job, err, s, out, blocks_per_sm, b);
 }
 
 }  // namespace kcv

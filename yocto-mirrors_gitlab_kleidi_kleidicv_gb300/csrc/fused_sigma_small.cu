@@ -1,11 +1,12 @@
 #include "fused_inst.cuh"
 namespace kcv {
-bool launch_fused_sigma_small(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out, int *o) {
+bool launch_fused_sigma_small(const FilterJob &j, int *e, cudaStream_t s, cudaError_t *out, int *o,
+                        const BatchLaunch *b) {
   if (j.mode != MODE_SIGMA) return false;
   switch (j.ksize) {
-    case 3: return dispatch_channels<MODE_SIGMA, 3>(j, e, s, out, o);
-    case 5: return dispatch_channels<MODE_SIGMA, 5>(j, e, s, out, o);
-    case 7: return dispatch_channels<MODE_SIGMA, 7>(j, e, s, out, o);
+    case 3: return dispatch_channels<MODE_SIGMA, 3>(j, e, s, out, o, b);
+    case 5: return dispatch_channels<MODE_SIGMA, 5>(j, e, s, out, o, b);
+    case 7: return dispatch_channels<MODE_SIGMA, 7>(j, e, s, out, o, b);
   }
   return false;
 }

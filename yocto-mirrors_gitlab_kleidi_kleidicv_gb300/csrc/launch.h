@@ -7,6 +7,18 @@
 
 namespace kcv {
 
+// A batched launch of one (mode, size, channels) instantiation: `ntiles`
+// tiles of the device job table `jobs`, claimed through *next_tile (0 at
+// launch), `grid` CTAs of 128 threads with `smem` bytes of shared memory.
+struct BatchLaunch {
+  const FilterJob *jobs;
+  const BatchTile *tiles;
+  int ntiles;
+  int *next_tile;
+  size_t smem;
+  int grid;
+};
+
 // Dynamic shared memory the fused kernel needs for `job`'s tiling.
 size_t fused_smem_bytes(const FilterJob &job);
 
@@ -22,13 +34,25 @@ int fused_blocks_per_sm(const FilterJob &job);
 // Per-family dispatchers (one translation unit each); return false if the
 // (mode, ksize, channels) combination is not theirs.  With blocks_per_sm set
 // they only report the occupancy instead of launching.
-bool launch_fused_binom(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_sigma_small(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_sigma_9(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_sigma_15(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_sigma_21(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
-bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm);
+bool launch_fused_binom(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_sigma_small(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_sigma_9(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_sigma_15(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_sigma_21(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
+
+// `rep` is any job of the instantiation (host copy): it selects the kernel.
+cudaError_t launch_fused_batch(const FilterJob &rep, const BatchLaunch &b, int *err_flag,
+                               cudaStream_t stream);
+int fused_batch_blocks_per_sm(const FilterJob &rep, const BatchLaunch &b);
 
 // Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
 // generated kernel whose weights do not sum to 256).  `scratch` holds the
