@@ -310,6 +310,55 @@ def batch_submit(requests, ctx=None):
     return err, [int(st[i]) for i in range(n)]
 
 
+# --- serving loop ----------------------------------------------------------
+
+class Server:
+    """kleidicv_gpu_server_t: continuous batching over a capped device pool."""
+
+    def __init__(self, device=0, pool_limit_bytes=0, max_inflight_batches=0, max_batch_requests=0,
+                 max_queue=0):
+        cfg = ServerConfig(pool_limit_bytes, max_inflight_batches, max_batch_requests, max_queue)
+        h = ctypes.c_void_p()
+        err = lib().kleidicv_gpu_server_create(ctypes.byref(cfg), device, ctypes.byref(h))
+        if err != OK:
+            raise RuntimeError(f"kleidicv_gpu_server_create failed: {ERROR_NAMES.get(err, err)}")
+        self.handle = h
+
+    def alloc(self, nbytes: int) -> int:
+        return lib().kleidicv_gpu_server_alloc(self.handle, nbytes) or 0
+
+    def free(self, ptr: int):
+        lib().kleidicv_gpu_server_free(self.handle, ptr)
+
+    def submit(self, request):
+        """Returns (error, id)."""
+        rid = ctypes.c_uint64()
+        err = lib().kleidicv_gpu_server_submit(self.handle, ctypes.byref(request), ctypes.byref(rid))
+        return err, rid.value
+
+    def poll(self, capacity=256, timeout_ms=0):
+        buf = (Completion * capacity)()
+        n = lib().kleidicv_gpu_server_poll(self.handle, buf, capacity, timeout_ms)
+        return [(c.id, c.status, c.arrival_s, c.admitted_s, c.completed_s) for c in buf[:n]]
+
+    def now(self) -> float:
+        return lib().kleidicv_gpu_server_now(self.handle)
+
+    def drain(self) -> int:
+        return lib().kleidicv_gpu_server_drain(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().kleidicv_gpu_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # --- torch helpers ---------------------------------------------------------
 
 def ptr(t):
