@@ -61,6 +61,10 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sections", default="c1,batched,pyramid,serving",
+                    help="extra measurements added to the line (comma list, or 'none')")
+    ap.add_argument("--serving-seconds", type=float, default=3.0)
+    ap.add_argument("--serving-rate", type=float, default=2000.0)
     return ap.parse_args()
 
 
@@ -377,6 +381,378 @@ def cpu_baseline(calls, passes, outputs=None):
 
 
 # ----------------------------------------------------------------------------
+# Further configurations of the workload description, reported beside the
+# headline sweep (rank 0, one GPU): the plain 1080p call, the uneven batch,
+# the pyramids and the serving loop.
+# ----------------------------------------------------------------------------
+
+def _events_time(torch, stream, fn, reps):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for i in range(reps):
+        fn(i)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def section_c1(torch, kcv, ctx, stream):
+    """1920x1080x1 u8, 5x5 binomial (sigma 0), REPLICATE, row stride w+64, seed 0."""
+    from oracle import oracle
+
+    w, h, stride = 1920, 1080, 1920 + 64
+    rng = np.random.default_rng(0)
+    host = rng.integers(0, 256, (h, stride), dtype=np.uint8)
+    nb = 40  # 40 x 2 x 2.1 MB > L2
+    srcs = [torch.from_numpy(host).cuda() for _ in range(nb)]
+    dsts = [torch.zeros((h, stride), dtype=torch.uint8, device="cuda") for _ in range(nb)]
+
+    def call(i):
+        e = kcv.gaussian_blur_u8(srcs[i % nb].data_ptr(), stride, dsts[i % nb].data_ptr(), stride, w, h, 1,
+                                 5, 5, 0.0, 0.0, kcv.REPLICATE, ctx)
+        assert e == kcv.OK, e
+
+    for i in range(5):
+        call(i)
+    ms = _events_time(torch, stream, call, 200)
+    _, want = oracle.gaussian_blur_u8(host, w, h, 1, 5, 0.0, kcv.REPLICATE,
+                                      dst=np.zeros((h, stride), np.uint8))
+    got = dsts[0].cpu().numpy()
+    return {"config": "1920x1080x1 u8 5x5 sigma 0 REPLICATE, stride w+64, seed 0",
+            "us_per_call": round(ms * 1e3, 2), "mpix_s": round(w * h / (ms * 1e-3) / 1e6, 1),
+            "hbm_gbs": round(2 * w * h / (ms * 1e-3) / 1e9, 1),
+            "bit_exact_vs_oracle": bool(np.array_equal(got[:, :w], want[:, :w]))}
+
+
+def _log_uniform(rng, lo, hi):
+    return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+
+
+def section_batched(torch, kcv, ctx, stream, cores):
+    """512 u8 images (seed 2): w 64-4096, h 64-2160 log-uniform, C in {1,3,4},
+    Gaussian k in {3,5,7,15}, sigma 0.5-4, random border: one CUDA-graph
+    launch of the batch plan against 512 plain calls and the CPU oracle."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(2)
+    items = []
+    for _ in range(512):
+        w, h = _log_uniform(rng, 64, 4096), _log_uniform(rng, 64, 2160)
+        c = int(rng.choice([1, 3, 4]))
+        k = int(rng.choice([3, 5, 7, 15]))
+        sigma = float(rng.uniform(0.5, 4.0))
+        border = int(rng.choice([kcv.REPLICATE, kcv.REFLECT, kcv.WRAP, kcv.REVERSE]))
+        host = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+        src = torch.from_numpy(host).cuda()
+        dst = torch.empty_like(src)
+        items.append((host, src, dst, w, h, c, k, sigma, border))
+    mpix = sum(it[3] * it[4] for it in items) / 1e6
+    nbytes = sum(2 * it[0].nbytes for it in items)
+    reqs = [kcv.make_request(kcv.OP_GAUSSIAN_BLUR_U8, it[1].data_ptr(), it[3] * it[5], it[2].data_ptr(),
+                             it[3] * it[5], it[3], it[4], it[5], it[6], it[6], it[7], it[7], border_type=it[8])
+            for it in items]
+    t0 = time.perf_counter()
+    plan = kcv.BatchPlan(reqs, ctx)
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    assert all(st == kcv.OK for st in plan.statuses), plan.statuses
+    for _ in range(3):
+        assert plan.launch(True) == kcv.OK
+    graph_ms = _events_time(torch, stream, lambda i: plan.launch(True), 20)
+
+    def plain(i):
+        for it in items:
+            e = kcv.gaussian_blur_u8(it[1].data_ptr(), it[3] * it[5], it[2].data_ptr(), it[3] * it[5], it[3],
+                                     it[4], it[5], it[6], it[6], it[7], it[7], it[8], ctx)
+            assert e == kcv.OK
+
+    plain(0)
+    plain_ms = _events_time(torch, stream, plain, 3)
+    # Outputs of the batched launch against the oracle on a sample.
+    plan.launch(True)
+    torch.cuda.synchronize()
+    exact = True
+    for it in items[:8]:
+        _, want = oracle.gaussian_blur_u8(it[0], it[3], it[4], it[5], it[6], it[7], it[8], nthreads=cores)
+        exact &= bool(np.array_equal(it[2].cpu().numpy(), want))
+    sample = items[:24]
+    t0 = time.perf_counter()
+    for it in sample:
+        oracle.gaussian_blur_u8(it[0], it[3], it[4], it[5], it[6], it[7], it[8], nthreads=cores)
+    cpu_s = time.perf_counter() - t0
+    cpu_mpix = sum(it[3] * it[4] for it in sample) / 1e6
+    tiles = plan.tile_count()
+    plan.close()
+    return {"config": "512 u8 images seed 2: w 64-4096, h 64-2160 log-uniform, C {1,3,4}, k {3,5,7,15}, "
+                      "sigma 0.5-4, random border",
+            "images": 512, "mpix": round(mpix, 1), "tiles": tiles,
+            "graph_ms": round(graph_ms, 3), "graph_mpix_s": round(mpix / (graph_ms * 1e-3), 1),
+            "graph_hbm_gbs": round(nbytes / (graph_ms * 1e-3) / 1e9, 1),
+            "plain_calls_ms": round(plain_ms, 3), "plain_mpix_s": round(mpix / (plain_ms * 1e-3), 1),
+            "speedup_vs_plain": round(plain_ms / graph_ms, 2), "plan_build_ms": round(plan_ms, 2),
+            "cpu_oracle_mpix_s": round(cpu_mpix / cpu_s, 1), "cpu_sample": f"24 images, {cores} threads",
+            "bit_exact_vs_oracle_sample": exact}
+
+
+def _pyr_image(rng, w, h, c):
+    y, x = np.mgrid[0:h, 0:w]
+    base = 128 + 60 * np.sin(x / 17.0 + y / 29.0)
+    img = np.repeat(base[:, :, None], c, axis=2) + rng.uniform(-40, 40, (h, w, c))
+    return np.clip(np.rint(img), 0, 255).astype(np.uint8).reshape(h, w * c)
+
+
+def section_pyramid(torch, kcv, ctx, stream):
+    """Seed 3: 8192x8192x1 and 4096x4096x3 through 5 blur_and_downsample
+    levels (REVERSE), and 64 pyramids of 1024x768x4 as batched plans."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(3)
+    out = {}
+    for (w, h, c) in ((8192, 8192, 1), (4096, 4096, 3)):
+        host = _pyr_image(rng, w, h, c)
+        src = torch.from_numpy(host).cuda()
+        sizes, ww, hh = [], w, h
+        for _ in range(5):
+            ww, hh = (ww + 1) // 2, (hh + 1) // 2
+            sizes.append((ww, hh))
+        dsts = [torch.empty((hh_, ww_ * c), dtype=torch.uint8, device="cuda") for ww_, hh_ in sizes]
+
+        def run(i):
+            e = kcv.build_pyramid_u8(src.data_ptr(), w * c, w, h, c, [d.data_ptr() for d in dsts],
+                                     [d.stride(0) for d in dsts], kcv.REVERSE, ctx)
+            assert e == kcv.OK
+
+        run(0)
+        ms = _events_time(torch, stream, run, 10)
+        _, l1 = oracle.blur_and_downsample_u8(host, w, h, c, kcv.REVERSE)
+        nbytes = host.nbytes + sum(d.numel() for d in dsts)
+        out[f"{w}x{h}x{c}"] = {"ms": round(ms, 3), "mpix_s_level0": round(w * h / (ms * 1e-3) / 1e6, 1),
+                               "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                               "level1_bit_exact": bool(np.array_equal(dsts[0].cpu().numpy(), l1))}
+    # 64 pyramids of 1024x768x4: one batch plan per level, replayed as graphs.
+    w, h, c = 1024, 768, 4
+    srcs = [torch.from_numpy(_pyr_image(rng, w, h, c)).cuda() for _ in range(64)]
+    levels, prev, pw, ph = [], srcs, w, h
+    plans = []
+    for _ in range(5):
+        nw, nh = (pw + 1) // 2, (ph + 1) // 2
+        outs = [torch.empty((nh, nw * c), dtype=torch.uint8, device="cuda") for _ in range(64)]
+        reqs = [kcv.make_request(kcv.OP_BLUR_AND_DOWNSAMPLE_U8, a.data_ptr(), pw * c, b.data_ptr(), nw * c, pw,
+                                 ph, c, border_type=kcv.REVERSE) for a, b in zip(prev, outs)]
+        plans.append(kcv.BatchPlan(reqs, ctx))
+        levels.append(outs)
+        prev, pw, ph = outs, nw, nh
+
+    def run_b(i):
+        for p in plans:
+            assert p.launch(True) == kcv.OK
+
+    run_b(0)
+    ms = _events_time(torch, stream, run_b, 10)
+    out["batched_64x1024x768x4"] = {"ms": round(ms, 3),
+                                    "mpix_s_level0": round(64 * w * h / (ms * 1e-3) / 1e6, 1)}
+    for p in plans:
+        p.close()
+    return out
+
+
+def section_serving(torch, kcv, seconds, rate):
+    """Seed 4: Poisson arrivals at `rate` requests/s for `seconds`; 0.60
+    gaussian_blur_u8 / 0.25 separable_filter_2d_u16 / 0.15
+    blur_and_downsample_u8; w 320-7680, h 240-4320 log-uniform, C {1,3,4},
+    Gaussian k {3,5,7,15}, separable 5x5, random border; images resident in the
+    server's 40 GB pool.  Requests draw from 48 resident source images of those
+    shapes; every request gets its own output buffer."""
+    rng = np.random.default_rng(4)
+    srv = kcv.Server(0, pool_limit_bytes=40 << 30, max_inflight_batches=4, max_batch_requests=256)
+    templates = []
+    for _ in range(48):
+        u = rng.random()
+        op = "gauss" if u < 0.60 else ("sep" if u < 0.85 else "bd")
+        w, h = _log_uniform(rng, 320, 7680), _log_uniform(rng, 240, 4320)
+        c = int(rng.choice([1, 3, 4]))
+        dtype = np.uint16 if op == "sep" else np.uint8
+        host = rng.integers(0, np.iinfo(dtype).max + 1, (h, w * c), dtype=dtype)
+        ptr = srv.alloc(host.nbytes)
+        assert ptr, "pool exhausted"
+        staging = torch.from_numpy(host.view(np.uint8).reshape(-1)).cuda()
+        _copy_device(ptr, staging.data_ptr(), host.nbytes)
+        del staging
+        templates.append(dict(op=op, w=w, h=h, c=c, dtype=dtype, src=ptr, free=[]))
+    torch.cuda.synchronize()
+
+    def out_bytes(tp):
+        es = np.dtype(tp["dtype"]).itemsize
+        if tp["op"] == "bd":
+            return ((tp["w"] + 1) // 2) * ((tp["h"] + 1) // 2) * tp["c"]
+        return tp["w"] * tp["h"] * tp["c"] * es
+
+    def make_req(tp, dst):
+        es = np.dtype(tp["dtype"]).itemsize
+        if tp["op"] == "gauss":
+            k = int(rng.choice([3, 5, 7, 15]))
+            sigma = float(rng.uniform(0.5, 4.0))
+            return kcv.make_request(kcv.OP_GAUSSIAN_BLUR_U8, tp["src"], tp["w"] * tp["c"], dst, tp["w"] * tp["c"],
+                                    tp["w"], tp["h"], tp["c"], k, k, sigma, sigma,
+                                    border_type=int(rng.choice([1, 2, 3, 4])))
+        if tp["op"] == "sep":
+            return kcv.make_request(kcv.OP_SEPARABLE_U16, tp["src"], tp["w"] * tp["c"] * es, dst,
+                                    tp["w"] * tp["c"] * es, tp["w"], tp["h"], tp["c"], 5, 5,
+                                    kernel_x=list(rng.integers(0, 5, 5)), kernel_y=list(rng.integers(0, 5, 5)),
+                                    border_type=int(rng.choice([1, 2, 3, 4])))
+        ow = (tp["w"] + 1) // 2
+        return kcv.make_request(kcv.OP_BLUR_AND_DOWNSAMPLE_U8, tp["src"], tp["w"] * tp["c"], dst, ow * tp["c"],
+                                tp["w"], tp["h"], tp["c"], border_type=int(rng.choice([1, 2, 3, 4])))
+
+    n = int(seconds * rate)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    choice = rng.integers(0, len(templates), n)
+    pending = {}
+    lat, mpix_done, busy = [], 0.0, 0
+    reqs_kept = []
+    t_start = time.perf_counter()
+    i = 0
+    while i < n or pending:
+        now = time.perf_counter() - t_start
+        while i < n and arrivals[i] <= now:
+            tp = templates[choice[i]]
+            dst = tp["free"].pop() if tp["free"] else srv.alloc(out_bytes(tp))
+            assert dst, "pool exhausted"
+            req = make_req(tp, dst)
+            err, rid = srv.submit(req)
+            if err != kcv.OK:
+                busy += 1
+                tp["free"].append(dst)
+            else:
+                pending[rid] = (tp, dst)
+                if len(reqs_kept) < 2000:
+                    reqs_kept.append((tp, req))
+            i += 1
+        for rid, st, ta, tad, tc in srv.poll(256, timeout_ms=0):
+            tp, dst = pending.pop(rid)
+            tp["free"].append(dst)
+            lat.append((tc - ta) * 1e3)
+            ow, oh = ((tp["w"] + 1) // 2, (tp["h"] + 1) // 2) if tp["op"] == "bd" else (tp["w"], tp["h"])
+            mpix_done += ow * oh / 1e6
+        if i < n and not pending:
+            time.sleep(max(0.0, min(arrivals[i] - (time.perf_counter() - t_start), 0.0005)))
+    wall = time.perf_counter() - t_start
+    srv.drain()
+    lat = np.array(lat)
+    # The same requests as plain per-request calls back to back, and as one batch.
+    ctx = kcv.Context.for_torch(0)
+    stream = torch.cuda.current_stream()
+    sample = reqs_kept[:1000]
+    outs = []
+    for tp, req in sample:
+        outs.append(torch.empty(out_bytes(tp), dtype=torch.uint8, device="cuda"))
+    plain_reqs = []
+    for (tp, req), o in zip(sample, outs):
+        r = kcv.make_request(req.op, req.src, req.src_stride, o.data_ptr(), req.dst_stride, req.width, req.height,
+                             req.channels, req.kernel_width, req.kernel_height, req.sigma_x, req.sigma_y,
+                             list(req.kernel_x), list(req.kernel_y), req.border_type)
+        plain_reqs.append(r)
+    sample_mpix = sum((((tp["w"] + 1) // 2) * ((tp["h"] + 1) // 2) if tp["op"] == "bd" else tp["w"] * tp["h"])
+                      for tp, _ in sample) / 1e6
+
+    def plain(_):
+        for r in plain_reqs:
+            e = _plain_call(kcv, r, ctx)
+            assert e == kcv.OK, e
+
+    plain(0)
+    plain_ms = _events_time(torch, stream, plain, 1)
+    plan = kcv.BatchPlan(plain_reqs, ctx)
+    plan.launch(True)
+    batch_ms = _events_time(torch, stream, lambda _: plan.launch(True), 3)
+    plan.close()
+    ctx.close()
+    srv.close()
+    return {"config": f"Poisson {rate:.0f} req/s for {seconds:.1f} s (seed 4), mix 0.60/0.25/0.15, "
+                      "w 320-7680 h 240-4320 log-uniform, 48 resident source images, 40 GB pool",
+            "requests": n, "completed": int(len(lat)), "busy": busy,
+            "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "p999_ms": round(float(np.percentile(lat, 99.9)), 3),
+            "mpix_s": round(mpix_done / wall, 1),
+            "plain_per_request_mpix_s": round(sample_mpix / (plain_ms * 1e-3), 1),
+            "batched_mpix_s": round(sample_mpix / (batch_ms * 1e-3), 1),
+            "comparison_sample": f"first {len(sample)} requests"}
+
+
+def _plain_call(kcv, r, ctx):
+    if r.op == kcv.OP_GAUSSIAN_BLUR_U8:
+        return kcv.gaussian_blur_u8(r.src, r.src_stride, r.dst, r.dst_stride, r.width, r.height, r.channels,
+                                    r.kernel_width, r.kernel_height, r.sigma_x, r.sigma_y, r.border_type, ctx)
+    if r.op == kcv.OP_SEPARABLE_U16:
+        return kcv.separable_filter_2d("u16", r.src, r.src_stride, r.dst, r.dst_stride, r.width, r.height,
+                                       r.channels, list(r.kernel_x), 5, list(r.kernel_y), 5, r.border_type, ctx)
+    return kcv.blur_and_downsample_u8(r.src, r.src_stride, r.width, r.height, r.dst, r.dst_stride, r.channels,
+                                      r.border_type, ctx)
+
+
+def _copy_device(dst_ptr, src_ptr, nbytes):
+    """Device-to-device copy between raw pointers (cudaMemcpy through ctypes)."""
+    import ctypes
+
+    lib = _cudart()
+    lib.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    err = lib.cudaMemcpy(ctypes.c_void_p(dst_ptr), ctypes.c_void_p(src_ptr), ctypes.c_size_t(nbytes), 3)
+    assert err == 0, err
+
+
+_CUDART = None
+
+
+def _cudart():
+    import ctypes
+    import glob
+
+    global _CUDART
+    if _CUDART is None:
+        import torch
+
+        cands = glob.glob(os.path.join(os.path.dirname(torch.__file__), "lib", "libcudart.so*"))
+        cands += glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+        for c in cands:
+            try:
+                _CUDART = ctypes.CDLL(c)
+                break
+            except OSError:
+                continue
+        if _CUDART is None:
+            _CUDART = ctypes.CDLL("libcudart.so")
+    return _CUDART
+
+
+def run_sections(args, names):
+    import torch
+    import __graft_entry__ as ge
+
+    kcv = ge.package()
+    stream = torch.cuda.current_stream()
+    ctx = kcv.Context(torch.cuda.current_device(), stream.cuda_stream)
+    cores = os.cpu_count() or 1
+    out = {}
+    for name in names:
+        t0 = time.perf_counter()
+        try:
+            if name == "c1":
+                out[name] = section_c1(torch, kcv, ctx, stream)
+            elif name == "batched":
+                out[name] = section_batched(torch, kcv, ctx, stream, cores)
+            elif name == "pyramid":
+                out[name] = section_pyramid(torch, kcv, ctx, stream)
+            elif name == "serving":
+                out[name] = section_serving(torch, kcv, args.serving_seconds, args.serving_rate)
+        except Exception as e:  # a failed section must not lose the headline line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["section_seconds"] = round(time.perf_counter() - t0, 1)
+        torch.cuda.empty_cache()
+    ctx.close()
+    return out
+
+
+# ----------------------------------------------------------------------------
 
 def main():
     args = parse_args()
@@ -459,9 +835,12 @@ def main():
         cb, exact = cpu_baseline(calls, args.cpu_passes, res["outputs"])
         line["cpu_baseline"] = cb
         line["bit_exact_vs_oracle"] = exact
+    close()
+    if rank == 0 and world == 1 and args.sections != "none":
+        names = [n for n in args.sections.split(",") if n]
+        line.update(run_sections(args, names))
     if rank == 0:
         print(json.dumps(line), flush=True)
-    close()
     if world > 1:
         import torch
 
