@@ -209,6 +209,26 @@ def profiled_traffic():
     return None
 
 
+def max_over_ranks(x: float) -> float:
+    """Largest value of x over the ranks (a timing: the slowest rank sets the
+    job's time).  NCCL reduces on the GPU, gloo on the host; one rank returns x."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, ms_per_step: float) -> float:
+    """Units per second of the whole job: every rank processes units_per_rank
+    per step (replicas), in the slowest rank's step time."""
+    return world * units_per_rank / (ms_per_step * 1e-3)
+
+
 def run_gpu(args, rank, world, calls, taps):
     import torch
     import __graft_entry__ as ge
@@ -287,11 +307,7 @@ def run_gpu(args, rank, world, calls, taps):
     for i in range(args.steps):
         for ci in range(len(calls)):
             per_call[ci].append(ev_calls[i][ci][0].elapsed_time(ev_calls[i][ci][1]))
-    ms_total = t_begin.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(t_begin.elapsed_time(t_end))
     ms_step = ms_total / args.steps
 
     # ---- end to end through the public calls with pinned host buffers.
@@ -321,11 +337,7 @@ def run_gpu(args, rank, world, calls, taps):
         e2e_step()
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_n
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_n)
     if ctx.synchronize() != kcv.OK:
         raise RuntimeError("end-to-end run failed")
 
@@ -805,7 +817,7 @@ def main():
     achieved = GAUSS_BYTES / (g_ms * 1e-3) / 1e9
     line = {
         "metric": METRIC,
-        "value": round(world * mpix / (res["ms_step"] * 1e-3), 1),
+        "value": round(whole_job_rate(mpix, world, res["ms_step"]), 1),
         "unit": METRIC,
         "n_gpus": world,
         "steps": args.steps,
@@ -826,7 +838,7 @@ def main():
                      "algorithmic_bytes_per_launch": GAUSS_BYTES,
                      "traffic": profiled_traffic()},
         "gpu_launches": res["launches"],
-        "e2e": {"value": round(world * mpix / (res["e2e_ms"] * 1e-3), 1), "unit": METRIC,
+        "e2e": {"value": round(whole_job_rate(mpix, world, res["e2e_ms"]), 1), "unit": METRIC,
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                 "ms_per_step": round(res["e2e_ms"], 4)},
         "clocks": res["clocks"],

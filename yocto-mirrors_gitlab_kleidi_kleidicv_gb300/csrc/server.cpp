@@ -210,6 +210,11 @@ kleidicv_error_t kleidicv_gpu_server_create(const kleidicv_gpu_server_config_t *
   if (cfg.max_inflight_batches <= 0) cfg.max_inflight_batches = 4;
   if (cfg.max_batch_requests <= 0) cfg.max_batch_requests = 256;
   if (cfg.max_queue <= 0) cfg.max_queue = 65536;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return KLEIDICV_GPU_ERROR_NO_DEVICE;
+  }
   auto *s = new kleidicv_gpu_server();
   s->cfg = cfg;
   s->device = device;
