@@ -508,6 +508,12 @@ kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx) {
   if (!ctx) return KLEIDICV_ERROR_NULL_POINTER;
   DeviceGuard guard(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (cudaStream_t s : ctx->branches) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  for (cudaEvent_t e : ctx->branch_events) cudaEventDestroy(e);
+  if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
   cudaFree(ctx->d_err);
   delete ctx;
   return KLEIDICV_OK;

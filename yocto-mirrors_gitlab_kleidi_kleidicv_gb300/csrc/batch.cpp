@@ -266,16 +266,28 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
   const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() +
                                           ((p->generic.empty() && p->copies.empty()) ? 0 : 1));
-  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
-  for (size_t b = 0; b < nbranch && ce == cudaSuccess; ++b) {
-    cudaStream_t st;
-    cudaEvent_t ev;
-    ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-    if (ce != cudaSuccess) break;
-    p->branches.push_back(st);
-    ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (ce != cudaSuccess) break;
-    p->joins.push_back(ev);
+  if (ce == cudaSuccess) {
+    // The context's branch streams and events, created once and shared.
+    std::lock_guard<std::mutex> lock(ctx->branch_mutex);
+    if (!ctx->fork_event) ce = cudaEventCreateWithFlags(&ctx->fork_event, cudaEventDisableTiming);
+    while (ce == cudaSuccess && ctx->branches.size() < nbranch) {
+      cudaStream_t st;
+      cudaEvent_t ev;
+      ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+      if (ce != cudaSuccess) break;
+      ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (ce != cudaSuccess) {
+        cudaStreamDestroy(st);
+        break;
+      }
+      ctx->branches.push_back(st);
+      ctx->branch_events.push_back(ev);
+    }
+    if (ce == cudaSuccess) {
+      p->fork = ctx->fork_event;
+      p->branches.assign(ctx->branches.begin(), ctx->branches.begin() + nbranch);
+      p->joins.assign(ctx->branch_events.begin(), ctx->branch_events.begin() + nbranch);
+    }
   }
   p->kernels_per_launch = p->groups.size() + 2 * p->generic.size();
   if (ce != cudaSuccess) {
@@ -325,10 +337,8 @@ kleidicv_error_t kleidicv_gpu_batch_plan_destroy(kleidicv_gpu_batch_plan_t *plan
   if (!plan) return KLEIDICV_ERROR_NULL_POINTER;
   DeviceGuard guard(plan->ctx->device);
   // Stream-ordered release: launches already enqueued finish first.
+  // The branch streams and events belong to the context.
   if (plan->exec) cudaGraphExecDestroy(plan->exec);
-  for (cudaStream_t s : plan->branches) cudaStreamDestroy(s);
-  for (cudaEvent_t ev : plan->joins) cudaEventDestroy(ev);
-  if (plan->fork) cudaEventDestroy(plan->fork);
   if (plan->dmem) ctx_free(plan->ctx, plan->dmem, plan->dmem_bytes);
   delete plan;
   return KLEIDICV_OK;

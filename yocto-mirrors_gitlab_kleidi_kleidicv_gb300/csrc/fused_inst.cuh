@@ -2,6 +2,7 @@
 #pragma once
 
 #include <algorithm>
+#include <mutex>
 
 #include "launch.h"
 #include "batch_kernel.cuh"
@@ -23,8 +24,20 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
       if (e != cudaSuccess) return e;
       battr_set = true;
     }
-    if (blocks_per_sm)
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, 128, batch->smem);
+    if (blocks_per_sm) {
+      // Cached per instantiation for the last shared-memory size asked.
+      static size_t cached_smem = ~static_cast<size_t>(0);
+      static int cached_occ = 0;
+      static std::mutex m;
+      std::lock_guard<std::mutex> lock(m);
+      if (cached_smem != batch->smem) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_occ, kern, 128, batch->smem);
+        if (e != cudaSuccess) return e;
+        cached_smem = batch->smem;
+      }
+      *blocks_per_sm = cached_occ;
+      return cudaSuccess;
+    }
     kern<<<static_cast<unsigned>(batch->grid), 128, batch->smem, stream>>>(
         batch->jobs, batch->tiles, batch->ntiles, batch->next_tile, err_flag);
     return cudaGetLastError();

@@ -7,6 +7,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "../../include/kleidicv_gpu.h"
 #include "kcv_job.h"
@@ -22,6 +23,13 @@ struct kleidicv_gpu_context {
   int *d_err = nullptr;  // device flag kernels set on a bounded-wait timeout
   int sm_count = 0;
   cudaError_t last_cuda_error = cudaSuccess;
+  // Streams and events the batch plans of this context fork onto (created on
+  // first use, shared by all plans: every launch orders them through events
+  // recorded on `stream`).
+  std::mutex branch_mutex;
+  std::vector<cudaStream_t> branches;
+  std::vector<cudaEvent_t> branch_events;
+  cudaEvent_t fork_event = nullptr;
 };
 
 namespace kcv {
