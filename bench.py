@@ -599,7 +599,7 @@ def section_pyramid(torch, kcv, ctx, stream):
     return out
 
 
-def section_serving(torch, kcv, seconds, rate):
+def section_serving(torch, kcv, seconds, rate, inflight=4, batch_requests=256):
     """Seed 4: Poisson arrivals at `rate` requests/s for `seconds`; 0.60
     gaussian_blur_u8 / 0.25 separable_filter_2d_u16 / 0.15
     blur_and_downsample_u8; w 320-7680, h 240-4320 log-uniform, C {1,3,4},
@@ -608,7 +608,7 @@ def section_serving(torch, kcv, seconds, rate):
     shapes, each with a ring of 16 output buffers (a buffer is reused 16
     requests of its image later, long after that request completed)."""
     rng = np.random.default_rng(4)
-    srv = kcv.Server(0, pool_limit_bytes=40 << 30, max_inflight_batches=4, max_batch_requests=256)
+    srv = kcv.Server(0, pool_limit_bytes=40 << 30, max_inflight_batches=inflight, max_batch_requests=batch_requests)
     templates = []
     for _ in range(48):
         u = rng.random()
@@ -711,7 +711,8 @@ def section_serving(torch, kcv, seconds, rate):
     ctx.close()
     srv.close()
     out = {"config": f"Poisson {rate:.0f} req/s for {seconds:.1f} s (seed 4), mix 0.60/0.25/0.15, "
-                     "w 320-7680 h 240-4320 log-uniform, 48 resident source images, 40 GB pool"}
+                     "w 320-7680 h 240-4320 log-uniform, 48 resident source images, 40 GB pool, "
+                     f"{inflight} batches in flight, <= {batch_requests} requests per batch"}
     out.update(main_run)
     out.update({"plain_per_request_mpix_s": round(sample_mpix / (plain_ms * 1e-3), 1),
                 "batched_mpix_s": round(batched_mpix_s, 1), "comparison_sample": f"first {len(sample)} requests",

@@ -391,8 +391,9 @@ void encode_tma(FilterJob &j) {
            CUDA_SUCCESS;
   };
   const cuuint32_t rb = static_cast<cuuint32_t>(j.stage_rows);
-  if (!enc(&j.tmap, wide, rb) || !enc(&j.tmap_row, wide, 1u) || !enc(&j.tmap_wrap, false, rb) ||
-      !enc(&j.tmap_wrap_row, false, 1u))
+  if (!enc(&j.tmap, wide, rb) || !enc(&j.tmap_row, wide, 1u)) return;
+  // The byte-unit wrap maps serve only a WRAP border (the far end of the row).
+  if (j.border == BORDER_WRAP && (!enc(&j.tmap_wrap, false, rb) || !enc(&j.tmap_wrap_row, false, 1u)))
     return;
   j.box_lbw = wide ? 11 : 8;
   j.use_tma = 1;
