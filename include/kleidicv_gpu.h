@@ -101,6 +101,15 @@ void kleidicv_gpu_context_fail_next_allocations(kleidicv_gpu_context_t *ctx,
                                                 int count);
 /* Number of this library's kernels launched through the context so far. */
 uint64_t kleidicv_gpu_context_launch_count(const kleidicv_gpu_context_t *ctx);
+/* Tuning knob (no reference counterpart): forces the fused kernels' tile
+ * shape for every later call on the context -- CTA threads (32..128, a
+ * multiple of 32), output rows per tile (0: balanced over one wave), rows per
+ * TMA stage and ring stages (0: the default depth; an explicit depth is
+ * raised to the ring depth rule's minimum).
+ * threads == 0 restores the committed autotune table / heuristic.  Used by
+ * the package's autotuner to measure candidate shapes. */
+kleidicv_error_t kleidicv_gpu_context_set_tile_shape(kleidicv_gpu_context_t *ctx, int threads,
+                                                     int tile_rows, int stage_rows, int stages);
 
 /* ------------------------------------------------------------------------ */
 /* Drop-in entry points.                                                    */

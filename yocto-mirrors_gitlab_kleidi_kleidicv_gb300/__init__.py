@@ -63,6 +63,7 @@ SIGNATURES = {
     "kleidicv_gpu_context_synchronize": (_i, [_vp]),
     "kleidicv_gpu_context_fail_next_allocations": (None, [_vp, _i]),
     "kleidicv_gpu_context_launch_count": (ctypes.c_uint64, [_vp]),
+    "kleidicv_gpu_context_set_tile_shape": (_i, [_vp, _i, _i, _i, _i]),
     "kleidicv_gpu_gaussian_blur_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i, _vp]),
     "kleidicv_gpu_gaussian_blur_u8_ex": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i,
                                               _u8, _vp]),
@@ -159,6 +160,9 @@ class Context:
 
     def launch_count(self) -> int:
         return lib().kleidicv_gpu_context_launch_count(self.handle)
+
+    def set_tile_shape(self, threads=0, tile_rows=0, stage_rows=4, stages=4) -> int:
+        return lib().kleidicv_gpu_context_set_tile_shape(self.handle, threads, tile_rows, stage_rows, stages)
 
     def fail_next_allocations(self, n: int):
         lib().kleidicv_gpu_context_fail_next_allocations(self.handle, n)

@@ -267,24 +267,20 @@ TileShape tile_shape_for(const FilterJob &j, int sm_count) {
   const int es = elem_size(j.mode);
   const long wcb = static_cast<long>(j.width) * j.channels * es;
   TileShape t{};
-  // Autotuned shapes (committed table) win when present.
-  if (lookup_tile_shape(j.mode, j.ksize, j.channels, wcb, j.out_height, &t.threads, &t.tile_rows,
-                        &t.stage_rows, &t.stages))
-    return t;
+  // Autotuned shapes (committed table) win when present; a row with threads
+  // 0 keeps the heuristic's warps per CTA below.
+  const bool tuned = lookup_tile_shape(j.mode, j.ksize, j.channels, wcb, j.out_height, &t.threads,
+                                       &t.tile_rows, &t.stage_rows, &t.stages);
+  if (tuned && t.threads > 0) return t;
   const int hc = halo_chunks(j);
   const long chunks = (wcb + kChunk - 1) / kChunk;  // 16-byte chunks per source row
   const int wi = 32 - 2 * hc;                        // interior chunks per warp
   const int warps = static_cast<int>(std::min<long>(4, std::max<long>(1, (chunks + wi - 1) / wi)));
   t.threads = 32 * warps;
-  const long strip_chunks = static_cast<long>(warps) * wi;
-  const long strips = j.mode == MODE_BLURDOWN
-                          ? (static_cast<long>(j.out_width) * j.channels + strip_chunks * 8 - 1) /
-                                (strip_chunks * 8)
-                          : (chunks + strip_chunks - 1) / strip_chunks;
-  (void)strips;
+  if (tuned) return t;
   t.tile_rows = 0;  // chosen from the measured occupancy (finish_plan)
   t.stage_rows = 4;
-  t.stages = 4;
+  t.stages = 0;     // the ring depth rule's default
   return t;
 }
 
@@ -310,7 +306,9 @@ static void fix_ring(FilterJob &j) {
     const int g = std::gcd(step, rb);
     int need = 1;
     for (int o = 0; o < rb; o += g) need = std::max(need, (o + in_rows - 1) / rb + 1);
-    ns = std::max(j.stages, need + 2);
+    // Explicit stage counts (autotune table, tuning knob) need only the
+    // safety minimum; the default keeps two stages of copies in flight.
+    ns = j.stages > 0 ? std::max(j.stages, need) : need + 2;
     if (ns <= 16 || rb >= 64) break;
   }
   j.stage_rows = rb;
@@ -450,7 +448,12 @@ kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
                                                 p.row_bytes, p.rows, cudaMemcpyDeviceToDevice,
                                                 ctx->stream));
     case Prepared::FUSED: {
-      plan_fused(p.fused, ctx->sm_count);
+      if (ctx->tune_threads > 0) {
+        TileShape t{ctx->tune_threads, ctx->tune_tile_rows, ctx->tune_stage_rows, ctx->tune_stages};
+        apply_tile_shape(p.fused, t);
+      } else {
+        plan_fused(p.fused, ctx->sm_count);
+      }
       encode_tma(p.fused);
       finish_plan(p.fused, ctx->sm_count);
       cudaError_t e = launch_fused(p.fused, ctx->d_err, ctx->stream);
@@ -555,6 +558,19 @@ void kleidicv_gpu_context_fail_next_allocations(kleidicv_gpu_context_t *ctx, int
 
 uint64_t kleidicv_gpu_context_launch_count(const kleidicv_gpu_context_t *ctx) {
   return ctx ? ctx->launches.load() : 0;
+}
+
+kleidicv_error_t kleidicv_gpu_context_set_tile_shape(kleidicv_gpu_context_t *ctx, int threads,
+                                                     int tile_rows, int stage_rows, int stages) {
+  if (!ctx) return KLEIDICV_ERROR_NULL_POINTER;
+  if (threads != 0 && (threads % 32 != 0 || threads < 32 || threads > 128 || tile_rows < 0 ||
+                       stage_rows < 1 || stages < 0 || stages > 16))
+    return KLEIDICV_ERROR_RANGE;
+  ctx->tune_threads = threads;
+  ctx->tune_tile_rows = tile_rows;
+  ctx->tune_stage_rows = stage_rows;
+  ctx->tune_stages = stages;
+  return KLEIDICV_OK;
 }
 
 static kleidicv_error_t run(kleidicv_gpu_context_t *ctx, kleidicv_error_t prep, Prepared &p) {

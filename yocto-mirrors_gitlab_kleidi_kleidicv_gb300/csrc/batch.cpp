@@ -188,8 +188,9 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
       }
       case Prepared::FUSED: {
         FilterJob j = pr.fused;
-        TileShape t = tile_shape_for(j, ctx->sm_count);
-        t.threads = kBatchThreads;
+        // The batched kernels run fixed 4-warp CTAs over 32-row tiles with the
+        // default ring (the autotune table is measured for whole-image calls).
+        TileShape t{kBatchThreads, 0, 4, 0};
         // Whole blocks of output rows; bands are counted in 16 bits.
         const int mb = block_out_rows(j.mode, j.ksize);
         const int rows_min = (j.out_height + 65534) / 65535;

@@ -26,6 +26,9 @@ struct kleidicv_gpu_context {
   // Streams and events the batch plans of this context fork onto (created on
   // first use, shared by all plans: every launch orders them through events
   // recorded on `stream`).
+  // Tile shape forced on every fused call of the context (the autotuner's
+  // knob; threads == 0: the autotune table or the heuristic decide).
+  int tune_threads = 0, tune_tile_rows = 0, tune_stage_rows = 0, tune_stages = 0;
   std::mutex branch_mutex;
   std::vector<cudaStream_t> branches;
   std::vector<cudaEvent_t> branch_events;
