@@ -1,14 +1,14 @@
 // Serving loop: continuous batching of filter requests.
 //
 // Clients allocate request images from the server's device pool, submit
-// requests at any time and poll completions.  A scheduler thread keeps up to
-// max_inflight_batches batches on the GPU, each on its own stream: whenever
-// a stream slot is free it admits the oldest queued requests (up to
+// requests at any time and poll completions.  Up to max_inflight_batches
+// batches are on the GPU at once, one per slot (a worker thread with its own
+// stream): a free worker admits the oldest queued requests (up to
 // max_batch_requests, and only as many as the pool's free bytes cover for the
-// batch's own device memory), builds a batch plan for them and launches it,
-// while the batches already on the GPU keep running.  Finished batches are
-// detected with events; their requests complete with the server-clock times
-// of arrival, admission and completion.
+// batch's own device memory), builds a batch plan for them and launches it
+// while the other slots' batches keep running.  Completion is detected with an
+// event; its requests complete with the server-clock times of arrival,
+// admission and completion.
 #include <stdint.h>
 
 #include <chrono>
@@ -64,7 +64,6 @@ struct kleidicv_gpu_server {
   int device = 0;
   Clock::time_point t0;
   std::vector<kleidicv_gpu_context_t *> slots;  // one context (stream) per in-flight batch
-  std::vector<bool> slot_busy;
   cudaStream_t alloc_stream = nullptr;
   cudaMemPool_t mempool = nullptr;
   size_t pool_used = 0;  // images + batch memory (guarded by mu)
@@ -73,128 +72,96 @@ struct kleidicv_gpu_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Pending> queue;
-  std::vector<Inflight> inflight;
   std::deque<kleidicv_gpu_completion_t> completions;
   uint64_t next_id = 1;
   size_t outstanding = 0;
+  int running = 0;  // batches on the GPU
   bool stop = false;
-  std::thread worker;
+  std::vector<std::thread> workers;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
-  void retire_finished() {  // holds mu
-    for (size_t i = 0; i < inflight.size();) {
-      Inflight &f = inflight[i];
-      const cudaError_t q = cudaEventQuery(f.done);
-      if (q == cudaErrorNotReady) {
-        ++i;
-        continue;
+  // Takes the oldest queued requests that the pool's free bytes cover (holds mu).
+  std::vector<Pending> take_batch(size_t *need) {
+    std::vector<Pending> batch;
+    *need = 0;
+    while (!queue.empty() && batch.size() < static_cast<size_t>(cfg.max_batch_requests)) {
+      batch.push_back(queue.front());
+      const size_t n = batch_bytes(batch);
+      if (pool_used + n > cfg.pool_limit_bytes && batch.size() > 1) {
+        batch.pop_back();
+        break;
       }
-      kleidicv_error_t batch_status = KLEIDICV_OK;
-      if (q != cudaSuccess) batch_status = KLEIDICV_GPU_ERROR_CUDA;
-      else if (kleidicv_gpu_context_synchronize(slots[f.slot]) != KLEIDICV_OK)
-        batch_status = KLEIDICV_GPU_ERROR_TIMEOUT;
+      *need = n;
+      queue.pop_front();
+    }
+    return batch;
+  }
+
+  // One worker per slot: take a batch, build and launch its plan on the
+  // slot's stream, wait for it, publish the completions.  The workers build
+  // plans concurrently, so a batch's preparation overlaps the other slots'
+  // batches on the GPU.
+  void work(int slot) {
+    kleidicv_gpu_context_t *ctx = slots[slot];
+    cudaStream_t stream = static_cast<cudaStream_t>(kleidicv_gpu_context_get_stream(ctx));
+    cudaEvent_t done = nullptr;
+    kcv::DeviceGuard guard(device);
+    const cudaError_t ev_err = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    std::unique_lock<std::mutex> lock(mu);
+    while (true) {
+      cv_work.wait(lock, [&] {
+        return (stop && queue.empty()) ||
+               (!queue.empty() && (running == 0 || pool_used + batch_bytes({queue.front()}) <=
+                                                       cfg.pool_limit_bytes));
+      });
+      if (queue.empty()) break;  // stopping, nothing left
+      size_t need = 0;
+      std::vector<Pending> batch = take_batch(&need);
+      pool_used += need;
+      ++running;
+      const double admitted = now();
+      lock.unlock();
+
+      std::vector<kleidicv_gpu_request_t> reqs(batch.size());
+      for (size_t k = 0; k < reqs.size(); ++k) reqs[k] = batch[k].req;
+      std::vector<kleidicv_error_t> statuses(reqs.size(), KLEIDICV_OK);
+      kleidicv_gpu_batch_plan_t *plan = nullptr;
+      kleidicv_error_t e = ev_err == cudaSuccess ? KLEIDICV_OK : KLEIDICV_GPU_ERROR_CUDA;
+      if (e == KLEIDICV_OK)
+        e = kleidicv_gpu_batch_plan_create(reqs.data(), reqs.size(), statuses.data(), &plan, ctx);
+      if (e == KLEIDICV_OK) e = kleidicv_gpu_batch_plan_launch(plan, 0, ctx);
+      if (e == KLEIDICV_OK && cudaEventRecord(done, stream) != cudaSuccess) e = KLEIDICV_GPU_ERROR_CUDA;
+      if (e == KLEIDICV_OK) {
+        // Poll (20 us) rather than block, so that the thread never holds the
+        // device lock of a blocking synchronisation.
+        cudaError_t q;
+        while ((q = cudaEventQuery(done)) == cudaErrorNotReady)
+          std::this_thread::sleep_for(std::chrono::microseconds(20));
+        if (q != cudaSuccess) e = KLEIDICV_GPU_ERROR_CUDA;
+        else if (kleidicv_gpu_context_synchronize(ctx) != KLEIDICV_OK) e = KLEIDICV_GPU_ERROR_TIMEOUT;
+      }
+      if (plan) kleidicv_gpu_batch_plan_destroy(plan);
       const double t = now();
-      for (size_t k = 0; k < f.reqs.size(); ++k) {
+
+      lock.lock();
+      for (size_t k = 0; k < batch.size(); ++k) {
         kleidicv_gpu_completion_t c;
-        c.id = f.reqs[k].id;
-        c.status = f.statuses[k] != KLEIDICV_OK ? f.statuses[k] : batch_status;
-        c.arrival_s = f.reqs[k].arrival_s;
-        c.admitted_s = f.admitted_s;
+        c.id = batch[k].id;
+        c.status = statuses[k] != KLEIDICV_OK ? statuses[k] : e;
+        c.arrival_s = batch[k].arrival_s;
+        c.admitted_s = admitted;
         c.completed_s = t;
         completions.push_back(c);
       }
-      outstanding -= f.reqs.size();
-      kleidicv_gpu_batch_plan_destroy(f.plan);
-      cudaEventDestroy(f.done);
-      pool_used -= f.reserved;
-      slot_busy[f.slot] = false;
-      inflight.erase(inflight.begin() + static_cast<long>(i));
+      outstanding -= batch.size();
+      pool_used -= need;
+      --running;
       cv_done.notify_all();
+      cv_work.notify_all();
     }
-  }
-
-  void run() {
-    std::unique_lock<std::mutex> lock(mu);
-    while (true) {
-      retire_finished();
-      if (stop && queue.empty() && inflight.empty()) break;
-      // Admit into a free slot: oldest requests first, bounded by the batch
-      // size and by the pool's free bytes.
-      int slot = -1;
-      for (size_t s = 0; s < slot_busy.size(); ++s)
-        if (!slot_busy[s]) {
-          slot = static_cast<int>(s);
-          break;
-        }
-      if (slot >= 0 && !queue.empty()) {
-        std::vector<Pending> batch;
-        size_t need = 0;
-        while (!queue.empty() && batch.size() < static_cast<size_t>(cfg.max_batch_requests)) {
-          batch.push_back(queue.front());
-          const size_t n = batch_bytes(batch);
-          if (pool_used + n > cfg.pool_limit_bytes && batch.size() > 1) {
-            batch.pop_back();
-            break;
-          }
-          need = n;
-          queue.pop_front();
-        }
-        if (pool_used + need > cfg.pool_limit_bytes && !inflight.empty()) {
-          // Not even one request fits: wait for a batch to finish.
-          for (auto it = batch.rbegin(); it != batch.rend(); ++it) queue.push_front(*it);
-        } else {
-          slot_busy[slot] = true;
-          pool_used += need;
-          const double admitted = now();
-          lock.unlock();
-          Inflight f;
-          f.reqs = std::move(batch);
-          f.slot = slot;
-          f.reserved = need;
-          f.admitted_s = admitted;
-          std::vector<kleidicv_gpu_request_t> reqs(f.reqs.size());
-          for (size_t k = 0; k < reqs.size(); ++k) reqs[k] = f.reqs[k].req;
-          f.statuses.assign(reqs.size(), KLEIDICV_OK);
-          kleidicv_error_t e = kleidicv_gpu_batch_plan_create(reqs.data(), reqs.size(),
-                                                              f.statuses.data(), &f.plan, slots[slot]);
-          if (e == KLEIDICV_OK) e = kleidicv_gpu_batch_plan_launch(f.plan, 0, slots[slot]);
-          if (e == KLEIDICV_OK &&
-              cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming) != cudaSuccess)
-            e = KLEIDICV_GPU_ERROR_CUDA;
-          if (e == KLEIDICV_OK &&
-              cudaEventRecord(f.done, kleidicv_gpu_context_get_stream_internal(slots[slot])) !=
-                  cudaSuccess)
-            e = KLEIDICV_GPU_ERROR_CUDA;
-          lock.lock();
-          if (e != KLEIDICV_OK) {
-            // The whole batch fails with the plan's error.
-            const double t = now();
-            for (const Pending &p : f.reqs)
-              completions.push_back({p.id, e, p.arrival_s, admitted, t});
-            outstanding -= f.reqs.size();
-            if (f.plan) kleidicv_gpu_batch_plan_destroy(f.plan);
-            if (f.done) cudaEventDestroy(f.done);
-            pool_used -= need;
-            slot_busy[slot] = false;
-            cv_done.notify_all();
-          } else {
-            inflight.push_back(std::move(f));
-          }
-          continue;
-        }
-      }
-      // Nothing to admit: sleep until a submission, or poll the batches on
-      // the GPU every 20 us.
-      if (inflight.empty())
-        cv_work.wait(lock, [&] { return stop || !queue.empty(); });
-      else
-        cv_work.wait_for(lock, std::chrono::microseconds(20));
-    }
-  }
-
-  static cudaStream_t kleidicv_gpu_context_get_stream_internal(kleidicv_gpu_context_t *c) {
-    return static_cast<cudaStream_t>(kleidicv_gpu_context_get_stream(c));
+    lock.unlock();
+    if (done) cudaEventDestroy(done);
   }
 };
 
@@ -235,28 +202,26 @@ kleidicv_error_t kleidicv_gpu_server_create(const kleidicv_gpu_server_config_t *
       return e;
     }
     s->slots.push_back(ctx);
-    s->slot_busy.push_back(false);
   }
   if (cudaStreamCreateWithFlags(&s->alloc_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaDeviceGetDefaultMemPool(&s->mempool, device) != cudaSuccess) {
     kleidicv_gpu_server_destroy(s);
     return KLEIDICV_GPU_ERROR_CUDA;
   }
-  s->worker = std::thread([s] { s->run(); });
+  for (int i = 0; i < cfg.max_inflight_batches; ++i) s->workers.emplace_back([s, i] { s->work(i); });
   *out = s;
   return KLEIDICV_OK;
 }
 
 kleidicv_error_t kleidicv_gpu_server_destroy(kleidicv_gpu_server_t *s) {
   if (!s) return KLEIDICV_ERROR_NULL_POINTER;
-  if (s->worker.joinable()) {
-    {
-      std::lock_guard<std::mutex> lock(s->mu);
-      s->stop = true;
-    }
-    s->cv_work.notify_all();
-    s->worker.join();
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->stop = true;
   }
+  s->cv_work.notify_all();
+  for (std::thread &t : s->workers)
+    if (t.joinable()) t.join();
   kcv::DeviceGuard guard(s->device);
   for (auto &a : s->allocations) cudaFreeAsync(a.first, s->alloc_stream);
   if (s->alloc_stream) {
