@@ -599,7 +599,7 @@ def section_pyramid(torch, kcv, ctx, stream):
     return out
 
 
-def section_serving(torch, kcv, seconds, rate, inflight=4, batch_requests=256):
+def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
     """Seed 4: Poisson arrivals at `rate` requests/s for `seconds`; 0.60
     gaussian_blur_u8 / 0.25 separable_filter_2d_u16 / 0.15
     blur_and_downsample_u8; w 320-7680, h 240-4320 log-uniform, C {1,3,4},

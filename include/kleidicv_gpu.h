@@ -266,8 +266,8 @@ typedef struct kleidicv_gpu_server kleidicv_gpu_server_t;
 
 typedef struct {
   size_t pool_limit_bytes;    /* device pool cap (0 = 40 GiB) */
-  int max_inflight_batches;   /* batches allowed on the GPU at once (0 = 4) */
-  int max_batch_requests;     /* requests per batch (0 = 256) */
+  int max_inflight_batches;   /* batches allowed on the GPU at once (0 = 3) */
+  int max_batch_requests;     /* requests per batch (0 = 512) */
   int max_queue;              /* pending requests before BUSY (0 = 65536) */
 } kleidicv_gpu_server_config_t;
 

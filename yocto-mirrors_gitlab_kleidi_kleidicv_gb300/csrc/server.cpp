@@ -174,8 +174,8 @@ kleidicv_error_t kleidicv_gpu_server_create(const kleidicv_gpu_server_config_t *
   kleidicv_gpu_server_config_t cfg{};
   if (config) cfg = *config;
   if (!cfg.pool_limit_bytes) cfg.pool_limit_bytes = 40ull << 30;
-  if (cfg.max_inflight_batches <= 0) cfg.max_inflight_batches = 4;
-  if (cfg.max_batch_requests <= 0) cfg.max_batch_requests = 256;
+  if (cfg.max_inflight_batches <= 0) cfg.max_inflight_batches = 3;
+  if (cfg.max_batch_requests <= 0) cfg.max_batch_requests = 512;
   if (cfg.max_queue <= 0) cfg.max_queue = 65536;
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
