@@ -350,6 +350,15 @@ kleidicv_error_t kleidicv_gpu_gaussian_blur_u8_noalloc(
     kleidicv_border_type_t border_type, void *stream);
 
 /* ------------------------------------------------------------------------ */
+/* Failure-path self-test (no reference counterpart): enqueues a kernel whose
+ * bounded wait on an mbarrier that nothing arrives at gives up after
+ * limit_ns (1 ns .. 1 s), as a fused kernel does when its copies never land.
+ * kleidicv_gpu_context_synchronize then reports KLEIDICV_GPU_ERROR_TIMEOUT
+ * once, and the context stays usable. */
+kleidicv_error_t kleidicv_gpu_selftest_bounded_wait(kleidicv_gpu_context_t *ctx,
+                                                    uint64_t limit_ns);
+
+/* ------------------------------------------------------------------------ */
 /* Introspection (used by tests): the Gaussian half kernel this library
  * derives from (kernel_size, sigma), with the reference's generator
  * (kleidicv/include/kleidicv/filters/sigma.h:27-79).  Returns 1 and fills

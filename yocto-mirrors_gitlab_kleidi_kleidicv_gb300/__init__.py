@@ -95,6 +95,7 @@ SIGNATURES = {
     "kleidicv_gpu_server_now": (ctypes.c_double, [_vp]),
     "kleidicv_gpu_server_drain": (_i, [_vp]),
     "kleidicv_gpu_gaussian_half_kernel": (_i, [_sz, _f, ctypes.POINTER(_u8)]),
+    "kleidicv_gpu_selftest_bounded_wait": (_i, [_vp, ctypes.c_uint64]),
     "kleidicv_gpu_gaussian_blur_u8_noalloc": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f,
                                                    _i, _vp]),
 }
