@@ -797,6 +797,8 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
       timed_out = true;
       atomicOr(err_flag, 1);
     }
+    // Interior warps of an interior stage: the copies are all there is.
+    if (use_tma && coop_lanes == 0u && j.border != BORDER_CONSTANT) return;
     const int rows = min(rb, in_rows - s * rb);
     if (!use_tma) {
 #pragma unroll 1
@@ -910,6 +912,8 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     // the buffer only after the __syncwarp of row m + 1, when every lane has
     // finished reading row m.
     const int mcount = min(M, orows - ob);
+    // This lane's destination chunk in the block's first row.
+    uint8_t *const dblock = dst_base + static_cast<int64_t>(oy0 + ob) * dst_stride + xb;
     static_for<0, M>([&](auto mc) {
       constexpr int Mi = decltype(mc)::value;
       uint32_t *vb = vwarp + (Mi & 1) * (kVRowBytes / 4);
@@ -923,9 +927,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
             make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
       }
       __syncwarp();
-      if (Mi < mcount) {
+      if constexpr (MODE == MODE_BLURDOWN) {
         uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + Mi) * dst_stride;
-        if constexpr (MODE == MODE_BLURDOWN) {
+        if (Mi < mcount) {
           if (emits && active) {
             const long ob8 = xb / 2;  // destination byte (= element) offset
             const long owc = static_cast<long>(j.out_width) * C;
@@ -941,18 +945,22 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
               }
             }
           }
-        } else {
-          uint4 r;
-          if constexpr (ModeTraits<MODE>::LANES)
-            r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
-          else
-            r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
-          if (full_store) *reinterpret_cast<uint4 *>(drow + xb) = r;
-          if (partial_store) {
-            const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
-            for (int k = 0; k < kChunk && xb + k < wcb; ++k)
-              drow[xb + k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
-          }
+        }
+      } else {
+        // Every row of the block is computed; rows past a partial last block
+        // of the band are not stored.
+        uint4 r;
+        if constexpr (ModeTraits<MODE>::LANES)
+          r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
+        else
+          r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
+        uint8_t *drow = dblock + Mi * dst_stride;
+        const bool row_ok = Mi < mcount;
+        if (full_store && row_ok) *reinterpret_cast<uint4 *>(drow) = r;
+        if (partial_store && row_ok) {
+          const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
+          for (int k = 0; k < kChunk && xb + k < wcb; ++k)
+            drow[k] = static_cast<uint8_t>(w4[k >> 2] >> (8 * (k & 3)));
         }
       }
     });
