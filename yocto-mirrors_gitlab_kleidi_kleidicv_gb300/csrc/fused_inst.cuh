@@ -65,8 +65,20 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long tiles = static_cast<long>(job.strips) * job.row_tiles;
   const long grid = std::max(1L, std::min(tiles, static_cast<long>(std::max(per_sm, 1)) * sms));
-  kern<<<static_cast<unsigned>(grid), job.threads, L.total, stream>>>(job, err_flag);
-  return cudaGetLastError();
+  // Programmatic stream serialization: this launch may begin while the
+  // previous kernel on the stream drains (the kernel waits for it before
+  // touching memory).
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(grid));
+  cfg.blockDim = dim3(static_cast<unsigned>(job.threads));
+  cfg.dynamicSmemBytes = L.total;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, job, err_flag);
 }
 
 template <int MODE, int K, bool NARROW>

@@ -16,6 +16,17 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
                : "memory");
 }
 
+// Programmatic dependent launch: let the next kernel of the stream start its
+// CTAs (they wait in grid_dependency_wait), and wait for every prerequisite
+// grid to complete with its memory visible.  Both are no-ops for a kernel
+// launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_inval(uint64_t *bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
 }

@@ -982,6 +982,9 @@ template <int MODE, int K, int C, bool NARROW>
 __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
     sepfused_kernel(const __grid_constant__ FilterJob job, int *err_flag) {
   extern __shared__ __align__(128) uint8_t smem[];
+  // The next call on the stream may start its CTAs as ours finish (they only
+  // fit where ours left room); everything it reads waits for our completion.
+  launch_dependents();
   if (job.use_tma) {
     if (threadIdx.x == 0) {
       prefetch_tensormap(&job.tmap);
@@ -1000,6 +1003,9 @@ __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
   bool timed_out = false;
   const TmaMaps maps{&job.tmap, &job.tmap_row, &job.tmap_wrap, &job.tmap_wrap_row};
   const int tiles = job.strips * job.row_tiles;
+  // The source may be the previous call's output: wait for that grid (set-up
+  // above overlapped its tail).
+  grid_dependency_wait();
   for (int t = blockIdx.x; t < tiles; t += gridDim.x)
     run_tile<MODE, K, C, NARROW>(job, maps, t % job.strips, t / job.strips, smem, gstage,
                                  err_flag, timed_out);
