@@ -198,6 +198,34 @@ kleidicv_error_t kleidicv_gpu_build_pyramid_u8(
     kleidicv_gpu_context_t *ctx);
 
 /* ------------------------------------------------------------------------ */
+/* Lucas-Kanade pyramid: the image and Scharr pyramids that
+ * kleidicv_build_optical_flow_pyr_lk_pyramid builds
+ * (kleidicv/include/kleidicv/kleidicv.h:361-364,
+ * kleidicv/src/analysis/build_optical_flow_pyr_lk_pyramid_api.cpp:13-48), in
+ * device memory.  Same arguments, validation order and level-count rule;
+ * level l >= 1 is blur_and_downsample (REVERSE) of level l-1.  Every level
+ * holds its image with a reflect-101 border of (window_width, window_height)
+ * pixels and the interleaved (dx, dy) Scharr derivatives (s16, 2 x channels
+ * per pixel) with a zero halo of the same size.  kleidicv_gpu_lk_pyramid_level
+ * returns DEVICE pointers to a level's interiors (the reference keeps its
+ * layout opaque; this accessor is the GPU handle's way to reach the data). */
+typedef struct kleidicv_gpu_lk_pyramid kleidicv_gpu_lk_pyramid_t;
+
+kleidicv_error_t kleidicv_gpu_build_optical_flow_pyr_lk_pyramid(
+    kleidicv_gpu_lk_pyramid_t **pyramid, const uint8_t *src, size_t src_stride, size_t width,
+    size_t height, size_t channels, size_t level_count, size_t window_width,
+    size_t window_height, kleidicv_gpu_context_t *ctx);
+/* kleidicv_optical_flow_pyr_lk_pyramid_release (kleidicv.h:377-378). */
+kleidicv_error_t kleidicv_gpu_optical_flow_pyr_lk_pyramid_release(
+    kleidicv_gpu_lk_pyramid_t *pyramid);
+size_t kleidicv_gpu_lk_pyramid_level_count(const kleidicv_gpu_lk_pyramid_t *pyramid);
+kleidicv_error_t kleidicv_gpu_lk_pyramid_level(const kleidicv_gpu_lk_pyramid_t *pyramid,
+                                               size_t level, size_t *width, size_t *height,
+                                               const uint8_t **image, size_t *image_stride,
+                                               const int16_t **scharr, size_t *scharr_stride,
+                                               size_t *border_width, size_t *border_height);
+
+/* ------------------------------------------------------------------------ */
 /* Batched execution: many independent filter requests of uneven sizes run
  * through one persistent kernel that walks a device-side tile work-list.  A
  * plan is built once (validation, tile list, tensor maps, tile shapes from

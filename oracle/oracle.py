@@ -133,6 +133,70 @@ def blur_and_downsample_u8(src, width, height, channels, border, *, ext=False, b
     return err, dst
 
 
+# --- LK optical-flow pyramid (kleidicv/include/kleidicv/analysis/build_optical_flow_pyr_lk_pyramid.h)
+
+MAX_LK_WINDOW = 2047  # KLEIDICV_MAX_OPTICAL_FLOW_PYR_LK_WINDOW_SIZE, kleidicv.h:119
+
+
+def lk_level_count(src_stride, width, height, channels, level_count, window_w, window_h):
+    """validate_and_compute_build_optical_flow_pyr_lk_levels (:18-58): (error, levels)."""
+    if (width == 0 or height == 0 or channels == 0 or channels > 4 or level_count == 0 or window_w <= 2
+            or window_h <= 2 or window_w > MAX_LK_WINDOW or window_h > MAX_LK_WINDOW):
+        return RANGE, 0
+    if height > 1 and src_stride < width * channels:
+        return RANGE, 0
+    n, w, h = 0, width, height
+    for _ in range(level_count):
+        n += 1
+        nw, nh = (w + 1) // 2, (h + 1) // 2
+        if nw <= window_w or nh <= window_h:
+            break
+        w, h = nw, nh
+    return OK, n
+
+
+def reflect_101_index(i, n):
+    """border_index_reflect_101 (:471-485): folds until inside [0, n)."""
+    if n <= 1:
+        return 0
+    while i < 0 or i >= n:
+        i = -i if i < 0 else 2 * n - i - 2
+    return i
+
+
+def lk_pyramid(src, width, height, channels, level_count, window_w, window_h):
+    """The pyramid of create() (:306-383): per level the image with a
+    reflect-101 border of (window_w, window_h) pixels and the interleaved
+    (dx, dy) Scharr derivatives (s16, width x height x 2C) computed from the
+    reflect-101 1-pixel ring.  Returns (error, [level dicts])."""
+    err, n = lk_level_count(src.strides[0] if src.ndim == 2 else width * channels, width, height, channels,
+                            level_count, window_w, window_h)
+    if err != OK:
+        return err, []
+    bw, bh = window_w, window_h
+    levels = []
+    img = np.ascontiguousarray(src[:height, : width * channels])
+    w, h = width, height
+    for lvl in range(n):
+        if lvl > 0:
+            e, img = blur_and_downsample_u8(img, w, h, channels, REVERSE)
+            assert e == OK
+            w, h = (w + 1) // 2, (h + 1) // 2
+        ys = np.array([reflect_101_index(y, h) for y in range(-bh, h + bh)])
+        xs = np.array([reflect_101_index(x, w) for x in range(-bw, w + bw)])
+        px = img.reshape(h, w, channels)
+        bordered = px[ys][:, xs].reshape(h + 2 * bh, (w + 2 * bw) * channels)
+        ring = px[[reflect_101_index(y, h) for y in range(-1, h + 1)]][:, [reflect_101_index(x, w) for x in range(-1, w + 1)]]
+        ring = ring.astype(np.int32)
+        dx = (3 * (ring[:-2, 2:] - ring[:-2, :-2]) + 10 * (ring[1:-1, 2:] - ring[1:-1, :-2]) +
+              3 * (ring[2:, 2:] - ring[2:, :-2]))
+        dy = (3 * (ring[2:, :-2] - ring[:-2, :-2]) + 10 * (ring[2:, 1:-1] - ring[:-2, 1:-1]) +
+              3 * (ring[2:, 2:] - ring[:-2, 2:]))
+        scharr = np.stack([dx, dy], axis=-1).astype(np.int16).reshape(h, w * channels * 2)
+        levels.append(dict(width=w, height=h, image=bordered, scharr=scharr))
+    return OK, levels
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv)
     print(LIB_PATH)

@@ -51,3 +51,47 @@ def pyr_sizes(w, h, levels):
         w, h = (w + 1) // 2, (h + 1) // 2
         out.append((w, h))
     return out
+
+
+_CUDART = None
+
+
+def _cudart():
+    """The CUDA runtime through ctypes (raw device pointers that no tensor owns)."""
+    import ctypes
+    import glob
+    import os
+
+    global _CUDART
+    if _CUDART is None:
+        import torch
+
+        cands = glob.glob(os.path.join(os.path.dirname(torch.__file__), "lib", "libcudart.so*"))
+        cands += glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+        for c in cands:
+            try:
+                _CUDART = ctypes.CDLL(c)
+                break
+            except OSError:
+                continue
+        if _CUDART is None:
+            _CUDART = ctypes.CDLL("libcudart.so")
+        _CUDART.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    return _CUDART
+
+
+def copy_from_device(ptr: int, nbytes: int) -> np.ndarray:
+    """Device bytes at a raw pointer -> host uint8 array (synchronous)."""
+    import ctypes
+
+    out = np.empty(nbytes, np.uint8)
+    err = _cudart().cudaMemcpy(ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(ptr), ctypes.c_size_t(nbytes), 2)
+    assert err == 0, err
+    return out
+
+
+def read_strided(ptr: int, rows: int, row_bytes: int, stride: int) -> np.ndarray:
+    """rows x row_bytes bytes starting at a device pointer, rows `stride` apart."""
+    raw = copy_from_device(ptr, (rows - 1) * stride + row_bytes)
+    return np.stack([raw[r * stride: r * stride + row_bytes] for r in range(rows)]) if rows else \
+        np.zeros((0, row_bytes), np.uint8)

@@ -96,6 +96,13 @@ SIGNATURES = {
     "kleidicv_gpu_server_drain": (_i, [_vp]),
     "kleidicv_gpu_gaussian_half_kernel": (_i, [_sz, _f, ctypes.POINTER(_u8)]),
     "kleidicv_gpu_selftest_bounded_wait": (_i, [_vp, ctypes.c_uint64]),
+    "kleidicv_gpu_build_optical_flow_pyr_lk_pyramid": (_i, [ctypes.POINTER(_vp), _vp, _sz, _sz, _sz, _sz, _sz,
+                                                            _sz, _sz, _vp]),
+    "kleidicv_gpu_optical_flow_pyr_lk_pyramid_release": (_i, [_vp]),
+    "kleidicv_gpu_lk_pyramid_level_count": (_sz, [_vp]),
+    "kleidicv_gpu_lk_pyramid_level": (_i, [_vp, _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz),
+                                           ctypes.POINTER(_vp), ctypes.POINTER(_sz), ctypes.POINTER(_vp),
+                                           ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
     "kleidicv_gpu_gaussian_blur_u8_noalloc": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f,
                                                    _i, _vp]),
 }
@@ -253,6 +260,47 @@ def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst
     return lib().kleidicv_gpu_build_pyramid_u8(src, src_stride, src_width, src_height, channels, n,
                                                ctypes.cast(dp, ctypes.c_void_p),
                                                ctypes.cast(ds, ctypes.c_void_p), border_type, _h(ctx))
+
+
+# --- Lucas-Kanade pyramid ---------------------------------------------------
+
+class LKPyramid:
+    """kleidicv_gpu_lk_pyramid_t: per-level bordered images and Scharr pairs on the GPU."""
+
+    def __init__(self, src, src_stride, width, height, channels, level_count, window_width, window_height,
+                 ctx=None):
+        h = ctypes.c_void_p()
+        err = lib().kleidicv_gpu_build_optical_flow_pyr_lk_pyramid(ctypes.byref(h), src, src_stride, width, height,
+                                                                   channels, level_count, window_width,
+                                                                   window_height, _h(ctx))
+        self.error = err
+        self.handle = h if err == OK else None
+
+    def level_count(self) -> int:
+        return lib().kleidicv_gpu_lk_pyramid_level_count(self.handle)
+
+    def level(self, i):
+        """(width, height, image_ptr, image_stride, scharr_ptr, scharr_stride, border_w, border_h)."""
+        vals = [_sz() for _ in range(2)]
+        img, sch = _vp(), _vp()
+        istr, sstr, bw, bh = _sz(), _sz(), _sz(), _sz()
+        err = lib().kleidicv_gpu_lk_pyramid_level(self.handle, i, ctypes.byref(vals[0]), ctypes.byref(vals[1]),
+                                                  ctypes.byref(img), ctypes.byref(istr), ctypes.byref(sch),
+                                                  ctypes.byref(sstr), ctypes.byref(bw), ctypes.byref(bh))
+        if err != OK:
+            raise RuntimeError(f"kleidicv_gpu_lk_pyramid_level: {ERROR_NAMES.get(err, err)}")
+        return (vals[0].value, vals[1].value, img.value, istr.value, sch.value, sstr.value, bw.value, bh.value)
+
+    def close(self):
+        if self.handle:
+            lib().kleidicv_gpu_optical_flow_pyr_lk_pyramid_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # --- batched execution -----------------------------------------------------
