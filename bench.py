@@ -61,7 +61,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="c1,batched,pyramid,serving",
+    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
     ap.add_argument("--serving-seconds", type=float, default=3.0)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
@@ -479,6 +479,45 @@ def section_c1(torch, kcv, ctx, stream):
             "bit_exact_vs_oracle": bool(np.array_equal(got[:, :w], want[:, :w]))}
 
 
+def section_sobel(torch, kcv, ctx, stream, cores):
+    """Sobel 3x3 d/dx and d/dy, u8 -> s16 (REPLICATE), 3840x2160 with 1 and 4
+    channels, seed 5: per-call time, HBM rate (1 byte read + 2 written per
+    element) against the measured copy bandwidth, and bit-exactness against
+    the CPU oracle."""
+    from oracle import oracle
+
+    peak, peak_kind = measured_hbm_peak()
+    rng = np.random.default_rng(5)
+    out = {"config": "3840x2160 u8 -> s16, REPLICATE, seed 5; rotating buffer sets > 2x L2",
+           "peak_source": f"{peak_kind} hbm_gbs"}
+    for c in (1, 4):
+        w, h = 3840, 2160
+        host = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+        per_set = 3 * w * h * c
+        nb = max(2, -(-300_000_000 // per_set))  # > 2x the 129 MB L2
+        srcs = [torch.from_numpy(host).cuda() for _ in range(nb)]
+        dsts = [torch.empty((h, w * c), dtype=torch.int16, device="cuda") for _ in range(nb)]
+        for name, fn, horizontal in (("dx", kcv.sobel_3x3_horizontal_s16_u8, True),
+                                     ("dy", kcv.sobel_3x3_vertical_s16_u8, False)):
+            def call(i, fn=fn):
+                e = fn(srcs[i % nb].data_ptr(), w * c, dsts[i % nb].data_ptr(), 2 * w * c, w, h, c, ctx)
+                assert e == kcv.OK, e
+
+            for i in range(5):
+                call(i)
+            ms = _events_time(torch, stream, call, 100)
+            call(0)
+            torch.cuda.synchronize()
+            _, want = oracle.sobel_3x3_s16_u8(host, w, h, c, horizontal, nthreads=cores)
+            gbs = per_set / (ms * 1e-3) / 1e9
+            out[f"{name}_c{c}"] = {"us_per_call": round(ms * 1e3, 2),
+                                   "mpix_s": round(w * h / (ms * 1e-3) / 1e6, 1),
+                                   "hbm_gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
+                                   "bit_exact_vs_oracle": bool(np.array_equal(dsts[0].cpu().numpy(), want))}
+        del srcs, dsts
+    return out
+
+
 def _log_uniform(rng, lo, hi):
     return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
 
@@ -800,6 +839,8 @@ def run_sections(args, names):
                 out[name] = section_batched(torch, kcv, ctx, stream, cores)
             elif name == "pyramid":
                 out[name] = section_pyramid(torch, kcv, ctx, stream)
+            elif name == "sobel":
+                out[name] = section_sobel(torch, kcv, ctx, stream, cores)
             elif name == "serving":
                 out[name] = section_serving(torch, kcv, args.serving_seconds, args.serving_rate)
         except Exception as e:  # a failed section must not lose the headline line

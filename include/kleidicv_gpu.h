@@ -27,6 +27,12 @@
  *                                        (kleidicv/src/filters/separable_filter_2d_api.cpp:67-75)
  *  kleidicv_gpu_blur_and_downsample_u8   kleidicv/include/kleidicv/kleidicv.h:2215-2218
  *                                        (kleidicv/src/filters/blur_and_downsample_api.cpp:40-48)
+ *  kleidicv_gpu_sobel_3x3_horizontal_s16_u8
+ *                                        kleidicv/include/kleidicv/kleidicv.h:2050-2052
+ *                                        (kleidicv/src/filters/sobel_api.cpp:37-43)
+ *  kleidicv_gpu_sobel_3x3_vertical_s16_u8
+ *                                        kleidicv/include/kleidicv/kleidicv.h:2006-2008
+ *                                        (kleidicv/src/filters/sobel_api.cpp:53-58)
  * and, with the same argument lists, the threaded variants
  *  kleidicv_thread_{gaussian_blur_u8,separable_filter_2d_u8,
  *  separable_filter_2d_u16,blur_and_downsample_u8}
@@ -136,6 +142,18 @@ kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8(
     const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height,
     uint8_t *dst, size_t dst_stride, size_t channels,
     kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+
+/* 3x3 Sobel derivatives, u8 -> s16, REPLICATE border (the reference's only
+ * one; there is no border argument).  horizontal = d/dx: [1 2 1]^T x
+ * [-1 0 1]; vertical = d/dy: [-1 0 1]^T x [1 2 1].  width, height >= 2, else
+ * NOT_IMPLEMENTED; dst_stride must be even when height > 1 (ALIGNMENT). */
+kleidicv_error_t kleidicv_gpu_sobel_3x3_horizontal_s16_u8(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
+
+kleidicv_error_t kleidicv_gpu_sobel_3x3_vertical_s16_u8(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
 
 /* ------------------------------------------------------------------------ */
 /* Extensions (no reference counterpart; semantics defined by this library,

@@ -79,7 +79,7 @@ long ko_border_map(long i, long n, int border) {
 }
 
 /* ------------------------------------------------------------------------ */
-enum { M_BINOM, M_SIGMA, M_SEP_U8, M_SEP_U16, M_SEP_S16, M_BLURDOWN };
+enum { M_BINOM, M_SIGMA, M_SEP_U8, M_SEP_U16, M_SEP_S16, M_BLURDOWN, M_SOBEL_X, M_SOBEL_Y };
 
 typedef struct {
   int mode;
@@ -116,7 +116,9 @@ static int64_t load_elem(const ko_job *j, long row, long elem) {
 
 static void store_elem(const ko_job *j, long row, long elem, int64_t v) {
   uint8_t *p = j->dst + (size_t)row * j->dst_stride;
-  if (j->elem_size == 1) {
+  if (j->mode == M_SOBEL_X || j->mode == M_SOBEL_Y) {
+    ((int16_t *)p)[elem] = (int16_t)v; /* u8 source, s16 destination */
+  } else if (j->elem_size == 1) {
     p[elem] = (uint8_t)v;
   } else if (j->mode == M_SEP_S16) {
     ((int16_t *)p)[elem] = (int16_t)v;
@@ -165,6 +167,12 @@ static int64_t vertical(const ko_job *j, const int64_t *s) {
       /* Saturating u32 accumulation (separable_filter_2d_neon.cpp:140-158). */
       for (int t = 0; t < k; ++t) acc += j->wy[t] * s[t];
       return acc > 0xFFFFFFFFLL ? 0xFFFFFFFFLL : acc;
+    case M_SOBEL_X:
+    case M_SOBEL_Y:
+      /* s16 row buffer: [1 2 1] or [-1 0 1] (sobel_neon.cpp:36-53, 95-109);
+       * |sum| <= 1020, so the reference's narrowing never wraps. */
+      for (int t = 0; t < k; ++t) acc += j->wy[t] * s[t];
+      return acc;
     case M_SEP_S16:
       /* Extension: product of tap 0, then saturating s32 adds in tap order. */
       acc = j->wy[0] * s[0];
@@ -205,6 +213,11 @@ static int64_t horizontal(const ko_job *j, const int64_t *v, long x) {
       return acc > 0xFF ? 0xFF : acc;
     case M_SEP_U16:
       return acc > 0xFFFF ? 0xFFFF : acc;
+    case M_SOBEL_X:
+    case M_SOBEL_Y:
+      /* [-1 0 1] or [1 2 1] of the row buffer (sobel_neon.cpp:58-69,
+       * 114-127); |result| <= 1020. */
+      return acc;
     case M_SEP_S16:
       if (acc > INT16_MAX) return INT16_MAX;
       if (acc < INT16_MIN) return INT16_MIN;
@@ -548,6 +561,60 @@ int ko_blur_and_downsample_u8(const uint8_t *src, size_t src_stride,
   j.dst_stride = dst_stride;
   j.elem_size = 1;
   return run_job(&j, nthreads);
+}
+
+/* ------------------------------------------------------------------------ */
+/* sobel_api.cpp:22-31 (sobel_is_implemented, filters/sobel.h:30-33), then
+ * sobel_neon.cpp:131-162 / :165-196: src and dst pointer/stride checks (a u8
+ * stride cannot be misaligned), image size, channels, then a separable 3x3
+ * pass with the REPLICATE border. */
+static int sobel_run(int mode, const uint8_t *src, size_t src_stride,
+                     int16_t *dst, size_t dst_stride, size_t width,
+                     size_t height, size_t channels, int nthreads) {
+  if (!(width >= 2 && height >= 2)) return KO_NOT_IMPLEMENTED;
+  if (!src) return KO_NULL_POINTER;
+  if (!dst) return KO_NULL_POINTER;
+  if (stride_misaligned(dst_stride, height, 2)) return KO_ALIGNMENT;
+  if (!image_size_ok(width, height)) return KO_RANGE;
+  if (channels > KO_MAX_CHANNELS) return KO_NOT_IMPLEMENTED;
+
+  static const int64_t smooth[3] = {1, 2, 1}, diff[3] = {-1, 0, 1};
+  ko_job j;
+  memset(&j, 0, sizeof(j));
+  j.mode = mode;
+  j.ksize = 3;
+  for (int t = 0; t < 3; ++t) {
+    j.wy[t] = mode == M_SOBEL_X ? smooth[t] : diff[t];
+    j.wx[t] = mode == M_SOBEL_X ? diff[t] : smooth[t];
+  }
+  j.border = KO_BORDER_REPLICATE;
+  j.width = width;
+  j.height = height;
+  j.channels = channels;
+  j.out_width = width;
+  j.out_height = height;
+  j.src = src;
+  j.src_stride = src_stride;
+  j.dst = (uint8_t *)dst;
+  j.dst_stride = dst_stride;
+  j.elem_size = 1;
+  return run_job(&j, nthreads);
+}
+
+int ko_sobel_3x3_horizontal_s16_u8(const uint8_t *src, size_t src_stride,
+                                   int16_t *dst, size_t dst_stride,
+                                   size_t width, size_t height,
+                                   size_t channels, int nthreads) {
+  return sobel_run(M_SOBEL_X, src, src_stride, dst, dst_stride, width, height,
+                   channels, nthreads);
+}
+
+int ko_sobel_3x3_vertical_s16_u8(const uint8_t *src, size_t src_stride,
+                                 int16_t *dst, size_t dst_stride, size_t width,
+                                 size_t height, size_t channels,
+                                 int nthreads) {
+  return sobel_run(M_SOBEL_Y, src, src_stride, dst, dst_stride, width, height,
+                   channels, nthreads);
 }
 
 /* ------------------------------------------------------------------------ */

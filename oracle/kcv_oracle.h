@@ -112,6 +112,16 @@ int ko_blur_and_downsample_u8(const uint8_t *src, size_t src_stride,
                               int border_type, int ext, int border_value,
                               int nthreads);
 
+/* 3x3 Sobel derivatives, u8 -> s16, REPLICATE border (sobel_api.cpp:22-76):
+ * horizontal = [1 2 1]^T x [-1 0 1], vertical = [-1 0 1]^T x [1 2 1]. */
+int ko_sobel_3x3_horizontal_s16_u8(const uint8_t *src, size_t src_stride,
+                                   int16_t *dst, size_t dst_stride,
+                                   size_t width, size_t height,
+                                   size_t channels, int nthreads);
+int ko_sobel_3x3_vertical_s16_u8(const uint8_t *src, size_t src_stride,
+                                 int16_t *dst, size_t dst_stride, size_t width,
+                                 size_t height, size_t channels, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,8 @@ def lib():
             getattr(_lib, name).argtypes = [vp, sz, vp, sz, sz, sz, sz, vp, sz, vp, sz, i, i, i, i]
         _lib.ko_separable_filter_2d_s16.argtypes = [vp, sz, vp, sz, sz, sz, sz, vp, sz, vp, sz, i, i, i]
         _lib.ko_blur_and_downsample_u8.argtypes = [vp, sz, sz, sz, vp, sz, sz, i, i, i, i]
+        for name in ("ko_sobel_3x3_horizontal_s16_u8", "ko_sobel_3x3_vertical_s16_u8"):
+            getattr(_lib, name).argtypes = [vp, sz, vp, sz, sz, sz, sz, i]
     return _lib
 
 
@@ -130,6 +132,16 @@ def blur_and_downsample_u8(src, width, height, channels, border, *, ext=False, b
         dst = _out_like(src, width, height, channels, np.uint8, (width + 1) // 2, (height + 1) // 2)
     err = lib().ko_blur_and_downsample_u8(_ptr(src), _stride(src), width, height, _ptr(dst), _stride(dst),
                                           channels, border, int(ext), int(border_value), nthreads)
+    return err, dst
+
+
+def sobel_3x3_s16_u8(src, width, height, channels, horizontal, *, nthreads=1, dst=None):
+    """Sobel x (horizontal=True) or y derivative of a u8 image as s16
+    (kleidicv/src/filters/sobel_api.cpp:22-76, sobel_neon.cpp)."""
+    if dst is None and src is not None:
+        dst = _out_like(src, width, height, channels, np.int16)
+    fn = lib().ko_sobel_3x3_horizontal_s16_u8 if horizontal else lib().ko_sobel_3x3_vertical_s16_u8
+    err = fn(_ptr(src), _stride(src), _ptr(dst), _stride(dst), width, height, channels, nthreads)
     return err, dst
 
 

@@ -79,6 +79,8 @@ SIGNATURES = {
                                                      _sz, _i, _i16, _vp]),
     "kleidicv_gpu_blur_and_downsample_u8": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _vp]),
     "kleidicv_gpu_blur_and_downsample_u8_ex": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _u8, _vp]),
+    "kleidicv_gpu_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
+    "kleidicv_gpu_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
     "kleidicv_gpu_build_pyramid_u8": (_i, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _i, _vp]),
     "kleidicv_gpu_batch_plan_create": (_i, [ctypes.POINTER(Request), _sz, ctypes.POINTER(_i),
                                             ctypes.POINTER(_vp), _vp]),
@@ -250,6 +252,18 @@ def blur_and_downsample_u8(src, src_stride, src_width, src_height, dst, dst_stri
     return lib().kleidicv_gpu_blur_and_downsample_u8_ex(src, src_stride, src_width, src_height, dst,
                                                         dst_stride, channels, border_type,
                                                         border_value, _h(ctx))
+
+
+def sobel_3x3_horizontal_s16_u8(src, src_stride, dst, dst_stride, width, height, channels, ctx=None):
+    """kleidicv_sobel_3x3_horizontal_s16_u8 (kleidicv/src/filters/sobel_api.cpp:37-43)."""
+    return lib().kleidicv_gpu_sobel_3x3_horizontal_s16_u8(src, src_stride, dst, dst_stride, width, height,
+                                                          channels, _h(ctx))
+
+
+def sobel_3x3_vertical_s16_u8(src, src_stride, dst, dst_stride, width, height, channels, ctx=None):
+    """kleidicv_sobel_3x3_vertical_s16_u8 (kleidicv/src/filters/sobel_api.cpp:53-58)."""
+    return lib().kleidicv_gpu_sobel_3x3_vertical_s16_u8(src, src_stride, dst, dst_stride, width, height,
+                                                        channels, _h(ctx))
 
 
 def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst_strides,

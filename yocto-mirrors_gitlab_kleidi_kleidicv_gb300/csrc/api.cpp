@@ -261,6 +261,30 @@ kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t 
   return KLEIDICV_OK;
 }
 
+kleidicv_error_t prepare_sobel(bool horizontal, const uint8_t *src, size_t src_stride,
+                               int16_t *dst, size_t dst_stride, size_t width, size_t height,
+                               size_t channels, Prepared *out) {
+  // sobel_api.cpp:22-31 (sobel_is_implemented, filters/sobel.h:30-33), then
+  // the stripe checks of sobel_neon.cpp:135-141 (u8 source strides cannot be
+  // misaligned).
+  if (!(width >= 2 && height >= 2)) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!src) return KLEIDICV_ERROR_NULL_POINTER;
+  if (!dst) return KLEIDICV_ERROR_NULL_POINTER;
+  if (stride_misaligned(dst_stride, height, 2)) return KLEIDICV_ERROR_ALIGNMENT;
+  if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
+  if (channels > kMaxChannels) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+
+  *out = Prepared{};
+  if (channels == 0) return KLEIDICV_OK;
+  out->kind = Prepared::FUSED;
+  FilterJob &j = out->fused;
+  // The only border of both derivatives is REPLICATE (sobel_neon.cpp:159,193).
+  fill_common(j, src, src_stride, dst, dst_stride, width, height, channels, BORDER_REPLICATE, 0);
+  j.ksize = 3;
+  j.mode = horizontal ? MODE_SOBEL_X : MODE_SOBEL_Y;
+  return KLEIDICV_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Tiling.
 TileShape tile_shape_for(const FilterJob &j, int sm_count) {
@@ -686,6 +710,26 @@ kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8_ex(
   Prepared p;
   auto e = prepare_blurdown(src, src_stride, src_width, src_height, dst, dst_stride, channels,
                             border_type, true, border_value, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_sobel_3x3_horizontal_s16_u8(const uint8_t *src, size_t src_stride,
+                                                         int16_t *dst, size_t dst_stride,
+                                                         size_t width, size_t height,
+                                                         size_t channels,
+                                                         kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_sobel(true, src, src_stride, dst, dst_stride, width, height, channels, &p);
+  return run(ctx, e, p);
+}
+
+kleidicv_error_t kleidicv_gpu_sobel_3x3_vertical_s16_u8(const uint8_t *src, size_t src_stride,
+                                                       int16_t *dst, size_t dst_stride,
+                                                       size_t width, size_t height,
+                                                       size_t channels,
+                                                       kleidicv_gpu_context_t *ctx) {
+  Prepared p;
+  auto e = prepare_sobel(false, src, src_stride, dst, dst_stride, width, height, channels, &p);
   return run(ctx, e, p);
 }
 

@@ -17,7 +17,8 @@ static bool dispatch_fused(const FilterJob &job, int *err, cudaStream_t s, cudaE
          launch_fused_sigma_9(job, err, s, out, occ, b) ||
          launch_fused_sigma_15(job, err, s, out, occ, b) ||
          launch_fused_sigma_21(job, err, s, out, occ, b) ||
-         launch_fused_sep(job, err, s, out, occ, b) || launch_fused_blurdown(job, err, s, out, occ, b);
+         launch_fused_sep(job, err, s, out, occ, b) || launch_fused_blurdown(job, err, s, out, occ, b) ||
+         launch_fused_sobel(job, err, s, out, occ, b);
 }
 cudaError_t launch_fused(const FilterJob &job, int *err, cudaStream_t s) {
   cudaError_t out = cudaErrorInvalidValue;

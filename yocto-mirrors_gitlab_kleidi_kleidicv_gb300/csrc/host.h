@@ -75,6 +75,11 @@ kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t 
                                   size_t channels, int border, bool ext, int border_value,
                                   Prepared *out);
 
+// horizontal: the x derivative (sobel_3x3_horizontal), else the y derivative.
+kleidicv_error_t prepare_sobel(bool horizontal, const uint8_t *src, size_t src_stride,
+                               int16_t *dst, size_t dst_stride, size_t width, size_t height,
+                               size_t channels, Prepared *out);
+
 // Chooses the tile shape (autotune table, else heuristic) and fills the
 // derived tiling fields of a FUSED job.  sm_count sizes the grid.
 void plan_fused(FilterJob &j, int sm_count);

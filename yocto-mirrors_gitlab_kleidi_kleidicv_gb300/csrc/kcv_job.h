@@ -15,6 +15,8 @@ enum Mode : int32_t {
   MODE_SEP_U16 = 4,     // separable_filter_2d_u16, 5x5, saturating
   MODE_SEP_S16 = 5,     // separable_filter_2d_s16 (extension)
   MODE_BLURDOWN = 6,    // blur_and_downsample_u8
+  MODE_SOBEL_X = 7,     // sobel_3x3_horizontal_s16_u8: [1 2 1]^T x [-1 0 1]
+  MODE_SOBEL_Y = 8,     // sobel_3x3_vertical_s16_u8: [-1 0 1]^T x [1 2 1]
 };
 
 // Border codes: the kleidicv_border_type_t values.

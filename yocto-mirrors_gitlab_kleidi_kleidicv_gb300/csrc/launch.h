@@ -48,6 +48,8 @@ bool launch_fused_sep(const FilterJob &, int *, cudaStream_t, cudaError_t *, int
                         const BatchLaunch *);
 bool launch_fused_blurdown(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
                         const BatchLaunch *);
+bool launch_fused_sobel(const FilterJob &, int *, cudaStream_t, cudaError_t *, int *blocks_per_sm,
+                        const BatchLaunch *);
 
 // `rep` is any job of the instantiation (host copy): it selects the kernel.
 cudaError_t launch_fused_batch(const FilterJob &rep, const BatchLaunch &b, int *err_flag,

@@ -25,7 +25,8 @@
 // Every output byte equals the reference's: the arithmetic per mode follows
 // kleidicv/src/filters/gaussian_blur_fixed_neon.cpp (binomial 3/5/7/9 and
 // generated-sigma kernels), separable_filter_2d_neon.cpp (u8/u16 saturation)
-// and blur_and_downsample_neon.cpp, with the border offset tables of
+// blur_and_downsample_neon.cpp and sobel_neon.cpp (3x3 derivatives, u8 in,
+// s16 out: 32 destination bytes per chunk), with the border offset tables of
 // kleidicv/include/kleidicv/workspace/border_*.h restated as a single-fold
 // index map.
 #pragma once
@@ -56,6 +57,9 @@ template <int MODE>
 struct ModeTraits {
   static constexpr int ES = (MODE == MODE_SEP_U16 || MODE == MODE_SEP_S16) ? 2 : 1;
   static constexpr bool LANES = ES == 1;  // u8 data held as packed 16-bit lanes
+  static constexpr bool SOBEL = MODE == MODE_SOBEL_X || MODE == MODE_SOBEL_Y;
+  // Destination bytes per source byte: the Sobel derivatives widen u8 to s16.
+  static constexpr int OSCALE = SOBEL ? 2 : 1;
 };
 
 template <int MODE, int K, int C>
@@ -223,6 +227,13 @@ __device__ __forceinline__ uint32_t vtap(uint32_t acc, uint32_t x, const Taps &t
     return acc + static_cast<uint32_t>(Binomial<K>::c(T)) * x;  // <= 255 * 256
   } else if constexpr (MODE == MODE_BLURDOWN) {
     return acc + static_cast<uint32_t>(Binomial<5>::c(T)) * x;
+  } else if constexpr (MODE == MODE_SOBEL_X) {
+    // [1 2 1] (sobel_neon.cpp:33-45): lanes <= 1020.
+    return T == 1 ? acc + 2u * x : acc + x;
+  } else if constexpr (MODE == MODE_SOBEL_Y) {
+    // [-1 0 1] (sobel_neon.cpp:92-101), on lanes biased by +256 so that the
+    // difference stays inside its 16-bit lane: lanes in [1, 511].
+    return T == 0 ? acc - x : (T == 2 ? acc + x : acc);
   } else if constexpr (MODE == MODE_SEP_U8) {
     // Saturating u16 in the reference (separable_filter_2d_neon.cpp:38-56).
     // Taps are non-negative, so any lane reaching 255 forces a 255 output:
@@ -268,7 +279,8 @@ __device__ __forceinline__ void vertical_block(const uint8_t *lane_base, uint32_
   static_for<0, M>([&](auto mc) {
     constexpr int Mi = decltype(mc)::value;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[Mi][j] = MODE == MODE_SIGMA ? 0x00800080u : 0u;
+    for (int j = 0; j < 8; ++j)
+      acc[Mi][j] = MODE == MODE_SIGMA ? 0x00800080u : (MODE == MODE_SOBEL_Y ? 0x01000100u : 0u);
   });
   static_for<0, NIN>([&](auto ic) {
     constexpr int I = decltype(ic)::value;
@@ -398,6 +410,50 @@ __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const u
     });
   }
   return make_uint4(out[0], out[1], out[2], out[3]);
+}
+
+// Sobel derivatives: the 16 s16 outputs of the thread (32 bytes, o0 = elements
+// 0..7, o1 = 8..15).  Every per-lane result r in [-1020, 1020] is formed as
+// 0x8000 + r inside its 16-bit lane (no carry or borrow crosses lanes), and
+// flipping bit 15 turns that into r's two's-complement bits.
+//   X: V[x + C] - V[x - C] of the [1 2 1] vertical sums (sobel_neon.cpp:55-60);
+//   Y: V[x - C] + 2 V[x] + V[x + C] of the +256-biased [-1 0 1] vertical
+//      differences (sobel_neon.cpp:111-118), bias 4 * 256 removed.
+template <int MODE, int C>
+__device__ __forceinline__ void horizontal_sobel(const uint32_t *vlo_s, const uint32_t *vhi_s,
+                                                 int tid, uint4 &o0, uint4 &o1) {
+  using G = Geo<MODE, 3, C>;
+  constexpr int HW = G::HW, NW = G::NW;
+  uint32_t lo[NW], hi[NW];
+  const int base = 4 * tid - HW;
+#pragma unroll
+  for (int k = 0; k < NW; k += 4) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(vlo_s + base + k);
+    const uint4 b = *reinterpret_cast<const uint4 *>(vhi_s + base + k);
+    lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
+    hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
+  }
+  uint32_t acc[8];
+  static_for<0, 8>([&](auto jc) {
+    constexpr int J = decltype(jc)::value;
+    const uint32_t l = pair_at<HW, NW, J / 2, J % 2, -C>(lo, hi);
+    const uint32_t r = pair_at<HW, NW, J / 2, J % 2, C>(lo, hi);
+    if constexpr (MODE == MODE_SOBEL_X) {
+      acc[J] = r - l + 0x80008000u;
+    } else {
+      const uint32_t m = pair_at<HW, NW, J / 2, J % 2, 0>(lo, hi);
+      acc[J] = l + r + 2u * m + (0x8000u - 4u * 256u) * 0x00010001u;
+    }
+  });
+  // acc[2I] holds elements (4I, 4I + 2), acc[2I + 1] elements (4I + 1, 4I + 3).
+  uint32_t w[8];
+  static_for<0, 4>([&](auto ic) {
+    constexpr int I = decltype(ic)::value;
+    w[2 * I] = __byte_perm(acc[2 * I], acc[2 * I + 1], 0x5410) ^ 0x80008000u;
+    w[2 * I + 1] = __byte_perm(acc[2 * I], acc[2 * I + 1], 0x7632) ^ 0x80008000u;
+  });
+  o0 = make_uint4(w[0], w[1], w[2], w[3]);
+  o1 = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
 // u16 / s16 separable: the V row holds 8 32-bit elements per lane (u16
@@ -773,7 +829,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   if constexpr (MODE == MODE_SIGMA) {
 #pragma unroll
     for (int t = 0; t <= K / 2; ++t) tp.y[t] = static_cast<uint32_t>(j.wy[t]);
-  } else if constexpr (MODE != MODE_BINOM && MODE != MODE_BLURDOWN) {
+  } else if constexpr (MODE != MODE_BINOM && MODE != MODE_BLURDOWN && !ModeTraits<MODE>::SOBEL) {
 #pragma unroll
     for (int t = 0; t < K; ++t) {
       tp.y[t] = static_cast<uint32_t>(j.wy[t]);
@@ -913,7 +969,8 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     // finished reading row m.
     const int mcount = min(M, orows - ob);
     // This lane's destination chunk in the block's first row.
-    uint8_t *const dblock = dst_base + static_cast<int64_t>(oy0 + ob) * dst_stride + xb;
+    uint8_t *const dblock =
+        dst_base + static_cast<int64_t>(oy0 + ob) * dst_stride + xb * ModeTraits<MODE>::OSCALE;
     static_for<0, M>([&](auto mc) {
       constexpr int Mi = decltype(mc)::value;
       uint32_t *vb = vwarp + (Mi & 1) * (kVRowBytes / 4);
@@ -944,6 +1001,24 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
                   drow[ob8 + k] = static_cast<uint8_t>(w2[k >> 2] >> (8 * (k & 3)));
               }
             }
+          }
+        }
+      } else if constexpr (ModeTraits<MODE>::SOBEL) {
+        // 32 destination bytes per chunk (s16 per source byte).
+        uint4 r0, r1;
+        horizontal_sobel<MODE, C>(vb, vb + 128, hlane, r0, r1);
+        uint8_t *drow = dblock + Mi * dst_stride;
+        const bool row_ok = Mi < mcount;
+        if (full_store && row_ok) {
+          *reinterpret_cast<uint4 *>(drow) = r0;
+          *reinterpret_cast<uint4 *>(drow + 16) = r1;
+        }
+        if (partial_store && row_ok) {
+          const uint32_t w8[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+          for (int k = 0; k < kChunk && xb + k < wcb; ++k) {
+            const uint32_t e = w8[k >> 1] >> (16 * (k & 1));
+            drow[2 * k] = static_cast<uint8_t>(e);
+            drow[2 * k + 1] = static_cast<uint8_t>(e >> 8);
           }
         }
       } else {
