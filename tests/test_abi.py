@@ -15,10 +15,17 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(REPO, "include", "kleidicv_gpu.h")
 
 
+HAL_HEADER = os.path.join(REPO, "include", "kleidicv_gpu_hal.h")
+
+
 def _declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(kleidicv_gpu_\w+)\s*\(", text)))
+    names = set(re.findall(r"\b(kleidicv_gpu_\w+)\s*\(", text))
+    # The HAL header's exported shim functions (its inline OpenCV wiring is not exported).
+    hal = re.sub(r"/\*.*?\*/", "", open(HAL_HEADER).read(), flags=re.S)
+    names |= set(re.findall(r"\b(kleidicv_gpu_hal_\w+)\s*\(", hal))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")

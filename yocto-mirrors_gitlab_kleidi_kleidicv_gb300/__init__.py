@@ -81,6 +81,16 @@ SIGNATURES = {
     "kleidicv_gpu_blur_and_downsample_u8_ex": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _u8, _vp]),
     "kleidicv_gpu_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
     "kleidicv_gpu_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
+    # OpenCV custom-HAL shim (include/kleidicv_gpu_hal.h): OpenCV's hook signatures.
+    "kleidicv_gpu_hal_separable_filter_2d": (_i, [_vp, _sz, _i, _vp, _sz, _i, _i, _i, _i, _i, _i, _i, _vp, _i,
+                                                  _vp, _i, _i, _i, _i, ctypes.c_double, _i]),
+    "kleidicv_gpu_hal_gaussian_blur_binomial": (_i, [_vp, _sz, _vp, _sz, _i, _i, _i, _i, _sz, _sz, _sz, _sz,
+                                                     _sz, _i]),
+    "kleidicv_gpu_hal_gaussian_blur": (_i, [_vp, _sz, _vp, _sz, _i, _i, _i, _i, _sz, _sz, _sz, _sz, _sz, _sz,
+                                            ctypes.c_double, ctypes.c_double, _i]),
+    "kleidicv_gpu_hal_pyrdown": (_i, [_vp, _sz, _i, _i, _vp, _sz, _i, _i, _i, _i, _i]),
+    "kleidicv_gpu_hal_sobel": (_i, [_vp, _sz, _vp, _sz, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
+                                    ctypes.c_double, ctypes.c_double, _i]),
     "kleidicv_gpu_build_pyramid_u8": (_i, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _i, _vp]),
     "kleidicv_gpu_batch_plan_create": (_i, [ctypes.POINTER(Request), _sz, ctypes.POINTER(_i),
                                             ctypes.POINTER(_vp), _vp]),
