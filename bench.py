@@ -61,7 +61,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,serving",
+    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,thread_api,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
     ap.add_argument("--serving-seconds", type=float, default=3.0)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
@@ -518,6 +518,46 @@ def section_sobel(torch, kcv, ctx, stream, cores):
     return out
 
 
+def section_thread_api(torch, kcv, cores):
+    """kleidicv_gpu_thread_gaussian_blur_u8 (KleidiCV's threaded-API contract:
+    host images, caller's scheduler, synchronous) on 3840x2160x4, 7x7, sigma
+    1.5, REVERSE, seed 1: host wall time per call from pageable and from
+    pinned host images, with the library's worker pool of 1 and of all host
+    threads driving the packing and unpacking."""
+    import time as _t
+
+    w, h, c = 3840, 2160, 4
+    rng = np.random.default_rng(1)
+    host = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+    out = {"config": "3840x2160x4 u8 7x7 sigma 1.5 REVERSE, seed 1; host wall time per call (upload, filter, "
+                     "download), median of 10 after 2 warm-up calls"}
+    lib = kcv.lib()
+    pinned_src = torch.from_numpy(host.copy()).pin_memory()
+    pinned_dst = torch.empty_like(pinned_src).pin_memory()
+    for threads in (1, cores):
+        pool = kcv.ThreadPool(threads)
+        for kind in ("pageable", "pinned"):
+            if kind == "pageable":
+                sp, dst = host.ctypes.data, np.zeros_like(host)
+                dp = dst.ctypes.data
+            else:
+                sp, dp = pinned_src.data_ptr(), pinned_dst.data_ptr()
+            times = []
+            for i in range(12):
+                t0 = _t.perf_counter()
+                e = lib.kleidicv_gpu_thread_gaussian_blur_u8(sp, w * c, dp, w * c, w, h, c, 7, 7, 1.5, 1.5,
+                                                             kcv.REVERSE, pool.mt)
+                t1 = _t.perf_counter()
+                assert e == kcv.OK, e
+                if i >= 2:
+                    times.append(t1 - t0)
+            ms = 1e3 * float(np.median(times))
+            out[f"{kind}_threads{threads}"] = {"ms_per_call": round(ms, 3),
+                                               "mpix_s": round(w * h / (ms * 1e-3) / 1e6, 1)}
+        pool.close()
+    return out
+
+
 def _log_uniform(rng, lo, hi):
     return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
 
@@ -839,6 +879,8 @@ def run_sections(args, names):
                 out[name] = section_batched(torch, kcv, ctx, stream, cores)
             elif name == "pyramid":
                 out[name] = section_pyramid(torch, kcv, ctx, stream)
+            elif name == "thread_api":
+                out[name] = section_thread_api(torch, kcv, cores)
             elif name == "sobel":
                 out[name] = section_sobel(torch, kcv, ctx, stream, cores)
             elif name == "serving":

@@ -16,6 +16,7 @@ HEADER = os.path.join(REPO, "include", "kleidicv_gpu.h")
 
 
 HAL_HEADER = os.path.join(REPO, "include", "kleidicv_gpu_hal.h")
+THREAD_HEADER = os.path.join(REPO, "include", "kleidicv_gpu_thread.h")
 
 
 def _declared_functions():
@@ -25,6 +26,8 @@ def _declared_functions():
     # The HAL header's exported shim functions (its inline OpenCV wiring is not exported).
     hal = re.sub(r"/\*.*?\*/", "", open(HAL_HEADER).read(), flags=re.S)
     names |= set(re.findall(r"\b(kleidicv_gpu_hal_\w+)\s*\(", hal))
+    thr = re.sub(r"/\*.*?\*/", "", open(THREAD_HEADER).read(), flags=re.S)
+    names |= set(re.findall(r"\b(kleidicv_gpu_thread_\w+)\s*\(", thr))
     return sorted(names)
 
 

@@ -1,0 +1,117 @@
+"""Threaded-API entries on the GPU: host images (pageable and pinned), device
+images and mixes, with the library's worker pool and with a serial scheduler
+written in Python, must give exactly the oracle's output; a scheduler that
+fails makes the call fail, and the next call is unaffected."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import __graft_entry__ as ge  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+kcv = ge.package()
+LIB = kcv.lib()
+POOL = None
+
+
+def setup_module():
+    global POOL
+    POOL = kcv.ThreadPool(8)
+
+
+def teardown_module():
+    POOL.close()
+
+
+class Img:
+    def __init__(self, arr, kind):
+        self.host = np.ascontiguousarray(arr)
+        self.kind = kind
+        raw = self.host.view(np.uint8)
+        if kind == "host":
+            self.ptr = self.host.ctypes.data
+        else:
+            self.t = torch.from_numpy(raw.copy())
+            self.t = self.t.pin_memory() if kind == "pinned" else self.t.cuda()
+            self.ptr = self.t.data_ptr()
+
+    def read(self):
+        if self.kind == "host":
+            return self.host
+        return self.t.cpu().numpy().view(self.host.dtype)
+
+
+COMBOS = [("host", "host"), ("pinned", "pinned"), ("device", "host"), ("host", "device"), ("pinned", "host")]
+
+
+def schedulers():
+    mt, keep = kcv.serial_scheduler()
+    return {"pool": (POOL.mt, None), "serial": (mt, keep)}
+
+
+@pytest.mark.parametrize("combo", COMBOS, ids=lambda c: f"{c[0]}-{c[1]}")
+@pytest.mark.parametrize("sched", ["pool", "serial"])
+def test_gaussian_threaded(combo, sched):
+    w, h, c = 3840, 2160, 4
+    rng = np.random.default_rng(1)
+    host = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+    src, dst = Img(host, combo[0]), Img(np.zeros_like(host), combo[1])
+    mt, keep = schedulers()[sched]
+    e = LIB.kleidicv_gpu_thread_gaussian_blur_u8(src.ptr, w * c, dst.ptr, w * c, w, h, c, 7, 7, 1.5, 1.5,
+                                                 kcv.REVERSE, mt)
+    assert e == kcv.OK
+    err, want = oracle.gaussian_blur_u8(host, w, h, c, 7, np.float32(1.5), kcv.REVERSE, nthreads=8)
+    assert np.array_equal(dst.read(), want)
+
+
+@pytest.mark.parametrize("combo", COMBOS, ids=lambda c: f"{c[0]}-{c[1]}")
+def test_other_ops_threaded(combo):
+    rng = np.random.default_rng(2)
+    w, h, c = 1001, 333, 3
+    h8 = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+    h16 = rng.integers(0, 65536, (h, w), dtype=np.uint16)
+    # separable u16 (1 channel)
+    kx = np.array([1, 2, 3, 2, 1], np.uint16)
+    ky = np.array([0, 1, 4, 1, 0], np.uint16)
+    src, dst = Img(h16, combo[0]), Img(np.zeros_like(h16), combo[1])
+    assert LIB.kleidicv_gpu_thread_separable_filter_2d_u16(src.ptr, 2 * w, dst.ptr, 2 * w, w, h, 1, kx.ctypes.data,
+                                                           5, ky.ctypes.data, 5, kcv.WRAP, POOL.mt) == kcv.OK
+    assert np.array_equal(dst.read(), oracle.separable_filter_2d(h16, w, h, 1, kx, ky, kcv.WRAP)[1])
+    # separable u8
+    k8 = np.array([1, 1, 2, 1, 1], np.uint8)
+    src, dst = Img(h8, combo[0]), Img(np.zeros_like(h8), combo[1])
+    assert LIB.kleidicv_gpu_thread_separable_filter_2d_u8(src.ptr, w * c, dst.ptr, w * c, w, h, c, k8.ctypes.data,
+                                                          5, k8.ctypes.data, 5, kcv.REFLECT, POOL.mt) == kcv.OK
+    assert np.array_equal(dst.read(), oracle.separable_filter_2d(h8, w, h, c, k8, k8, kcv.REFLECT)[1])
+    # blur and downsample
+    dw, dh = (w + 1) // 2, (h + 1) // 2
+    src, dst = Img(h8, combo[0]), Img(np.zeros((dh, dw * c), np.uint8), combo[1])
+    assert LIB.kleidicv_gpu_thread_blur_and_downsample_u8(src.ptr, w * c, w, h, dst.ptr, dw * c, c, kcv.REVERSE,
+                                                          POOL.mt) == kcv.OK
+    assert np.array_equal(dst.read(), oracle.blur_and_downsample_u8(h8, w, h, c, kcv.REVERSE)[1])
+    # sobel x and y
+    for horizontal, fn in ((True, LIB.kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8),
+                           (False, LIB.kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8)):
+        src, dst = Img(h8, combo[0]), Img(np.zeros((h, w * c), np.int16), combo[1])
+        assert fn(src.ptr, w * c, dst.ptr, 2 * w * c, w, h, c, POOL.mt) == kcv.OK
+        assert np.array_equal(dst.read(), oracle.sobel_3x3_s16_u8(h8, w, h, c, horizontal)[1])
+
+
+def test_failing_scheduler_fails_the_call():
+    @kcv.THREAD_PARALLEL
+    def refuses(callback, callback_data, parallel_data, task_count):
+        return 4  # ALLOCATION: the scheduler could not run the tasks
+
+    mt = kcv.ThreadMT(ctypes.cast(refuses, ctypes.c_void_p).value, None)
+    host = np.random.default_rng(3).integers(0, 256, (200, 300), dtype=np.uint8)
+    dst = np.zeros_like(host)
+    assert LIB.kleidicv_gpu_thread_gaussian_blur_u8(host.ctypes.data, 300, dst.ctypes.data, 300, 300, 200, 1, 5, 5,
+                                                    0.0, 0.0, kcv.REFLECT, mt) == kcv.ALLOCATION
+    assert LIB.kleidicv_gpu_thread_gaussian_blur_u8(host.ctypes.data, 300, dst.ctypes.data, 300, 300, 200, 1, 5, 5,
+                                                    0.0, 0.0, kcv.REFLECT, POOL.mt) == kcv.OK
+    assert np.array_equal(dst, oracle.gaussian_blur_u8(host, 300, 200, 1, 5, 0.0, kcv.REFLECT)[1])

@@ -1,0 +1,116 @@
+"""The threaded-API layer without a GPU: the library's worker pool fulfils
+KleidiCV's scheduler contract (kleidicv_thread.h:42-97: every task index run
+exactly once, the first failure reported, nothing run after the call
+returns), and the kleidicv_gpu_thread_* entries validate like the reference,
+reject a missing scheduler, and fail loudly without a device."""
+import ctypes
+import threading
+
+import numpy as np
+import pytest
+
+CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p)
+
+
+@pytest.fixture(scope="module")
+def lib(kcv):
+    return kcv.lib()
+
+
+@pytest.fixture(scope="module")
+def no_gpu():
+    try:
+        import torch
+
+        return not torch.cuda.is_available()
+    except ImportError:
+        return True
+
+
+@pytest.mark.parametrize("threads", [1, 2, 4, 8])
+def test_pool_runs_every_task_once(lib, kcv, threads):
+    pool = kcv.ThreadPool(threads)
+    try:
+        for count in (1, 3, 64, 1000):
+            seen = []
+            lock = threading.Lock()
+            tids = set()
+
+            @CB
+            def cb(begin, end, data):
+                with lock:
+                    seen.extend(range(begin, end))
+                    tids.add(threading.get_ident())
+                return 0
+
+            assert lib.kleidicv_gpu_thread_pool_parallel(cb, None, pool.handle, count) == 0
+            assert sorted(seen) == list(range(count))
+        assert lib.kleidicv_gpu_thread_pool_parallel(cb, None, pool.handle, 0) == 0
+    finally:
+        pool.close()
+
+
+def test_pool_reports_first_failure_and_stays_usable(lib, kcv):
+    pool = kcv.ThreadPool(4)
+    try:
+        @CB
+        def failing(begin, end, data):
+            return 3 if begin == 17 else 0  # RANGE from one task
+
+        @CB
+        def fine(begin, end, data):
+            return 0
+
+        for _ in range(20):
+            assert lib.kleidicv_gpu_thread_pool_parallel(failing, None, pool.handle, 40) == 3
+            assert lib.kleidicv_gpu_thread_pool_parallel(fine, None, pool.handle, 40) == 0
+        assert lib.kleidicv_gpu_thread_pool_parallel(None, None, pool.handle, 4) == 2
+        assert lib.kleidicv_gpu_thread_pool_parallel(fine, None, None, 4) == 2
+    finally:
+        pool.close()
+
+
+def test_pool_stress_many_small_calls(lib, kcv):
+    pool = kcv.ThreadPool(6)
+    total = [0]
+    lock = threading.Lock()
+
+    @CB
+    def cb(begin, end, data):
+        with lock:
+            total[0] += end - begin
+        return 0
+
+    try:
+        for i in range(300):
+            assert lib.kleidicv_gpu_thread_pool_parallel(cb, None, pool.handle, 1 + i % 7) == 0
+        assert total[0] == sum(1 + i % 7 for i in range(300))
+    finally:
+        pool.close()
+
+
+def test_entries_validate_then_need_a_scheduler(lib, kcv, oracle, no_gpu):
+    pool = kcv.ThreadPool(2)
+    none = kcv.ThreadMT(None, None)
+    a = np.zeros((16, 64), np.uint8)
+    b = np.zeros((16, 64), np.uint8)
+    g = lib.kleidicv_gpu_thread_gaussian_blur_u8
+    try:
+        # Validation first, whatever the scheduler (gaussian_blur_api.cpp order).
+        for mt in (none, pool.mt):
+            assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 4, 4, 0.0, 0.0, kcv.REFLECT, mt) == \
+                kcv.NOT_IMPLEMENTED
+            assert g(None, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT, mt) == kcv.NULL_POINTER
+            assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.CONSTANT, mt) == \
+                kcv.NOT_IMPLEMENTED
+        assert lib.kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8(a.ctypes.data, 64, b.ctypes.data, 63, 32, 16, 1,
+                                                                 pool.mt) == kcv.ALIGNMENT
+        # A valid call with no scheduler.
+        assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT, none) == \
+            kcv.NULL_POINTER
+        if no_gpu:
+            assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT, pool.mt) == \
+                kcv.ERROR_NO_DEVICE
+            assert not b.any()
+    finally:
+        pool.close()

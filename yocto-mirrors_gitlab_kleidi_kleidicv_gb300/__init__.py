@@ -48,6 +48,11 @@ class ServerConfig(ctypes.Structure):
                 ("max_queue", _i)]
 
 
+class ThreadMT(ctypes.Structure):
+    """kleidicv_thread_multithreading: the caller's scheduler (function pointer) and its data."""
+    _fields_ = [("parallel", _vp), ("parallel_data", _vp)]
+
+
 class Completion(ctypes.Structure):
     _fields_ = [("id", ctypes.c_uint64), ("status", _i), ("arrival_s", ctypes.c_double),
                 ("admitted_s", ctypes.c_double), ("completed_s", ctypes.c_double)]
@@ -81,6 +86,19 @@ SIGNATURES = {
     "kleidicv_gpu_blur_and_downsample_u8_ex": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _u8, _vp]),
     "kleidicv_gpu_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
     "kleidicv_gpu_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
+    # Threaded API (include/kleidicv_gpu_thread.h): host images, the caller's scheduler.
+    "kleidicv_gpu_thread_gaussian_blur_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i,
+                                                  ThreadMT]),
+    "kleidicv_gpu_thread_separable_filter_2d_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp, _sz,
+                                                        _i, ThreadMT]),
+    "kleidicv_gpu_thread_separable_filter_2d_u16": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp, _sz,
+                                                         _i, ThreadMT]),
+    "kleidicv_gpu_thread_blur_and_downsample_u8": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, ThreadMT]),
+    "kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, ThreadMT]),
+    "kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, ThreadMT]),
+    "kleidicv_gpu_thread_pool_create": (_i, [ctypes.POINTER(_vp), ctypes.c_uint]),
+    "kleidicv_gpu_thread_pool_destroy": (_i, [_vp]),
+    "kleidicv_gpu_thread_pool_parallel": (_i, [_vp, _vp, _vp, ctypes.c_uint]),
     # OpenCV custom-HAL shim (include/kleidicv_gpu_hal.h): OpenCV's hook signatures.
     "kleidicv_gpu_hal_separable_filter_2d": (_i, [_vp, _sz, _i, _vp, _sz, _i, _i, _i, _i, _i, _i, _i, _vp, _i,
                                                   _vp, _i, _i, _i, _i, ctypes.c_double, _i]),
@@ -262,6 +280,41 @@ def blur_and_downsample_u8(src, src_stride, src_width, src_height, dst, dst_stri
     return lib().kleidicv_gpu_blur_and_downsample_u8_ex(src, src_stride, src_width, src_height, dst,
                                                         dst_stride, channels, border_type,
                                                         border_value, _h(ctx))
+
+
+THREAD_CALLBACK = ctypes.CFUNCTYPE(_i, ctypes.c_uint, ctypes.c_uint, _vp)
+THREAD_PARALLEL = ctypes.CFUNCTYPE(_i, THREAD_CALLBACK, _vp, _vp, ctypes.c_uint)
+
+
+class ThreadPool:
+    """The library's worker pool implementing the kleidicv_thread_parallel
+    contract; `mt` is the kleidicv_thread_multithreading value to pass."""
+
+    def __init__(self, threads: int = 0):
+        h = _vp()
+        err = lib().kleidicv_gpu_thread_pool_create(ctypes.byref(h), threads)
+        if err != OK:
+            raise RuntimeError(f"kleidicv_gpu_thread_pool_create failed: {ERROR_NAMES.get(err, err)}")
+        self.handle = h.value
+        fn = ctypes.cast(lib().kleidicv_gpu_thread_pool_parallel, _vp).value
+        self.mt = ThreadMT(fn, self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().kleidicv_gpu_thread_pool_destroy(self.handle)
+            self.handle = None
+
+
+def serial_scheduler():
+    """A scheduler written in Python: runs every task range on the calling
+    thread (the reference's serial fallback).  Keep the returned pair alive
+    while it is in use."""
+
+    @THREAD_PARALLEL
+    def parallel(callback, callback_data, parallel_data, task_count):
+        return callback(0, task_count, callback_data)
+
+    return ThreadMT(ctypes.cast(parallel, _vp).value, None), parallel
 
 
 def sobel_3x3_horizontal_s16_u8(src, src_stride, dst, dst_stride, width, height, channels, ctx=None):

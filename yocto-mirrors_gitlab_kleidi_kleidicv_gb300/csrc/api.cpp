@@ -542,6 +542,7 @@ kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx) {
   }
   for (cudaEvent_t e : ctx->branch_events) cudaEventDestroy(e);
   if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
   cudaFree(ctx->d_err);
   delete ctx;
   return KLEIDICV_OK;

@@ -33,6 +33,10 @@ struct kleidicv_gpu_context {
   std::vector<cudaStream_t> branches;
   std::vector<cudaEvent_t> branch_events;
   cudaEvent_t fork_event = nullptr;
+  // Pinned host staging of the scheduler-driven (threaded-API) entries:
+  // grow-only, freed with the context.
+  void *pinned = nullptr;
+  size_t pinned_bytes = 0;
 };
 
 namespace kcv {

@@ -1,0 +1,431 @@
+// Threaded-API entries (include/kleidicv_gpu_thread.h): KleidiCV's
+// kleidicv_thread_* contract -- host images, a caller-provided scheduler,
+// synchronous return -- with the filter on the GPU and the scheduler's tasks
+// doing the host side of the transfers, plus a persistent worker pool that
+// implements the scheduler contract.
+#include "../../include/kleidicv_gpu_thread.h"
+
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "host.h"
+
+// ---------------------------------------------------------------------------
+// Worker pool (kleidicv_thread_parallel).  Every `parallel` call wakes all
+// workers; each takes task indices from a shared counter, and the call
+// returns once every worker has finished with this call's job, so a job's
+// callback is never run after its call returned.
+struct kleidicv_gpu_thread_pool {
+  struct Job {
+    kleidicv_thread_callback cb = nullptr;
+    void *data = nullptr;
+    unsigned count = 0;
+  };
+  std::vector<std::thread> workers;
+  std::mutex m, call;
+  std::condition_variable wake, done;
+  uint64_t generation = 0;
+  size_t finished = 0;
+  bool stop = false;
+  Job job;
+  std::atomic<unsigned> next{0};
+  std::atomic<int> error{KLEIDICV_OK};
+
+  void run(const Job &j) {
+    for (unsigned i; (i = next.fetch_add(1)) < j.count;) {
+      const kleidicv_error_t e = j.cb(i, i + 1, j.data);
+      if (e != KLEIDICV_OK) {
+        int expected = KLEIDICV_OK;
+        error.compare_exchange_strong(expected, static_cast<int>(e));
+      }
+    }
+  }
+  void worker() {
+    uint64_t seen = 0;
+    for (;;) {
+      Job j;
+      {
+        std::unique_lock<std::mutex> l(m);
+        wake.wait(l, [&] { return stop || generation != seen; });
+        if (stop) return;
+        seen = generation;
+        j = job;
+      }
+      run(j);
+      std::lock_guard<std::mutex> l(m);
+      if (++finished == workers.size()) done.notify_all();
+    }
+  }
+};
+
+namespace {
+
+using kcv::Prepared;
+
+bool device_accessible(const void *p, bool *pinned) {
+  cudaPointerAttributes a;
+  *pinned = false;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  *pinned = a.type == cudaMemoryTypeHost;
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Grows the context's pinned staging to `bytes`.
+bool pinned_staging(kleidicv_gpu_context_t *ctx, size_t bytes) {
+  if (ctx->pinned_bytes >= bytes) return true;
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  ctx->pinned = nullptr;
+  ctx->pinned_bytes = 0;
+  if (cudaHostAlloc(&ctx->pinned, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->pinned = nullptr;
+    return false;
+  }
+  ctx->pinned_bytes = bytes;
+  return true;
+}
+
+struct HostImage {
+  const uint8_t *ptr;
+  size_t stride, row_bytes, rows;
+};
+
+// One side (source or destination) of a threaded call.
+struct Side {
+  HostImage img;
+  bool on_device = false;  // device or managed memory: used in place
+  bool pinned = false;     // page-locked host memory: copied without packing
+  uint8_t *dev = nullptr;  // device image (pitch `pitch`)
+  uint8_t *stage = nullptr;  // pinned packing area (pitch `pitch`)
+  size_t pitch = 0, dev_bytes = 0;
+  unsigned rows_per_task = 1, tasks = 0;
+};
+
+void plan_tasks(Side &s) {
+  // Stripes of about 2 MiB, at most 1024 of them.
+  const size_t target = 2u << 20;
+  size_t rpt = std::max<size_t>(1, target / std::max<size_t>(s.img.row_bytes, 1));
+  rpt = std::max(rpt, (s.img.rows + 1023) / 1024);
+  s.rows_per_task = static_cast<unsigned>(rpt);
+  s.tasks = static_cast<unsigned>((s.img.rows + rpt - 1) / rpt);
+}
+
+struct Transfer {
+  kleidicv_gpu_context_t *ctx;
+  Side *side;
+  std::vector<cudaEvent_t> *events;
+};
+
+kleidicv_error_t cuda_fail(kleidicv_gpu_context_t *ctx, cudaError_t e) {
+  return kcv::cuda_status(ctx, e);
+}
+
+// Upload task t: pack its rows into pinned memory (pageable source) and
+// enqueue their host-to-device copy.
+kleidicv_error_t upload_task(unsigned begin, unsigned end, void *data) {
+  const Transfer &x = *static_cast<Transfer *>(data);
+  Side &s = *x.side;
+  kcv::DeviceGuard guard(x.ctx->device);
+  for (unsigned t = begin; t < end; ++t) {
+    const size_t r0 = static_cast<size_t>(t) * s.rows_per_task;
+    const size_t r1 = std::min(s.img.rows, r0 + s.rows_per_task);
+    cudaError_t e;
+    if (s.pinned) {
+      e = cudaMemcpy2DAsync(s.dev + r0 * s.pitch, s.pitch, s.img.ptr + r0 * s.img.stride,
+                            s.img.stride, s.img.row_bytes, r1 - r0, cudaMemcpyHostToDevice,
+                            x.ctx->stream);
+    } else {
+      for (size_t r = r0; r < r1; ++r)
+        memcpy(s.stage + r * s.pitch, s.img.ptr + r * s.img.stride, s.img.row_bytes);
+      e = cudaMemcpyAsync(s.dev + r0 * s.pitch, s.stage + r0 * s.pitch, (r1 - r0) * s.pitch,
+                          cudaMemcpyHostToDevice, x.ctx->stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(x.ctx, e);
+  }
+  return KLEIDICV_OK;
+}
+
+// Download task t: wait for its stripe's copy, then unpack it into dst.
+kleidicv_error_t download_task(unsigned begin, unsigned end, void *data) {
+  const Transfer &x = *static_cast<Transfer *>(data);
+  Side &s = *x.side;
+  kcv::DeviceGuard guard(x.ctx->device);
+  for (unsigned t = begin; t < end; ++t) {
+    const cudaError_t e = cudaEventSynchronize((*x.events)[t]);
+    if (e != cudaSuccess) return cuda_fail(x.ctx, e);
+    const size_t r0 = static_cast<size_t>(t) * s.rows_per_task;
+    const size_t r1 = std::min(s.img.rows, r0 + s.rows_per_task);
+    uint8_t *dst = const_cast<uint8_t *>(s.img.ptr);
+    for (size_t r = r0; r < r1; ++r)
+      memcpy(dst + r * s.img.stride, s.stage + r * s.pitch, s.img.row_bytes);
+  }
+  return KLEIDICV_OK;
+}
+
+using DeviceOp = std::function<kleidicv_error_t(const void *, size_t, void *, size_t,
+                                                kleidicv_gpu_context_t *)>;
+
+kleidicv_error_t run_threaded(kleidicv_error_t validation, const Prepared &p, HostImage src,
+                              HostImage dst, const DeviceOp &op,
+                              kleidicv_thread_multithreading mt) {
+  if (validation != KLEIDICV_OK) return validation;
+  if (!mt.parallel) return KLEIDICV_ERROR_NULL_POINTER;
+  if (p.kind == Prepared::NOTHING) return KLEIDICV_OK;
+  kleidicv_gpu_context_t *ctx = nullptr;
+  kleidicv_error_t e = kcv::resolve_context(ctx);
+  if (e != KLEIDICV_OK) return e;
+  kcv::DeviceGuard guard(ctx->device);
+
+  Side s, d;
+  s.img = src;
+  d.img = dst;
+  s.on_device = device_accessible(src.ptr, &s.pinned);
+  d.on_device = device_accessible(dst.ptr, &d.pinned);
+  auto pitch_of = [](size_t row_bytes) { return (row_bytes + 255) / 256 * 256; };
+  for (Side *x : {&s, &d}) {
+    if (x->on_device) {
+      x->dev = const_cast<uint8_t *>(x->img.ptr);
+      x->pitch = x->img.stride;
+    } else {
+      x->pitch = pitch_of(x->img.row_bytes);
+      x->dev_bytes = x->pitch * x->img.rows;
+      plan_tasks(*x);
+    }
+  }
+  const size_t stage_s = (!s.on_device && !s.pinned) ? s.pitch * s.img.rows : 0;
+  const size_t stage_d = (!d.on_device && !d.pinned) ? d.pitch * d.img.rows : 0;
+  if (stage_s + stage_d > 0) {
+    if (!pinned_staging(ctx, stage_s + stage_d)) return KLEIDICV_ERROR_ALLOCATION;
+    s.stage = static_cast<uint8_t *>(ctx->pinned);
+    d.stage = static_cast<uint8_t *>(ctx->pinned) + stage_s;
+  }
+  if (s.dev_bytes) s.dev = static_cast<uint8_t *>(kcv::ctx_alloc(ctx, s.dev_bytes));
+  if (d.dev_bytes) d.dev = static_cast<uint8_t *>(kcv::ctx_alloc(ctx, d.dev_bytes));
+  std::vector<cudaEvent_t> events;
+  auto finish = [&](kleidicv_error_t result) {
+    if (!s.on_device) kcv::ctx_free(ctx, s.dev, s.dev_bytes);
+    if (!d.on_device) kcv::ctx_free(ctx, d.dev, d.dev_bytes);
+    const kleidicv_error_t se = kleidicv_gpu_context_synchronize(ctx);
+    for (cudaEvent_t ev : events) cudaEventDestroy(ev);
+    return result != KLEIDICV_OK ? result : se;
+  };
+  if ((s.dev_bytes && !s.dev) || (d.dev_bytes && !d.dev)) return finish(KLEIDICV_ERROR_ALLOCATION);
+
+  // Upload phase: the scheduler runs the source stripes.
+  if (!s.on_device) {
+    Transfer x{ctx, &s, nullptr};
+    e = mt.parallel(upload_task, &x, mt.parallel_data, s.tasks);
+    if (e != KLEIDICV_OK) return finish(e);
+  }
+  e = op(s.dev, s.pitch, d.dev, d.pitch, ctx);
+  if (e != KLEIDICV_OK) return finish(e);
+  if (d.on_device) return finish(KLEIDICV_OK);
+  // Download phase: one copy and one event per destination stripe, then the
+  // scheduler unpacks stripes as their copies land.
+  events.resize(d.tasks, nullptr);
+  for (unsigned t = 0; t < d.tasks; ++t) {
+    const size_t r0 = static_cast<size_t>(t) * d.rows_per_task;
+    const size_t r1 = std::min(d.img.rows, r0 + d.rows_per_task);
+    cudaError_t ce = cudaEventCreateWithFlags(&events[t], cudaEventDisableTiming);
+    if (ce == cudaSuccess) {
+      if (d.pinned)
+        ce = cudaMemcpy2DAsync(const_cast<uint8_t *>(d.img.ptr) + r0 * d.img.stride, d.img.stride,
+                               d.dev + r0 * d.pitch, d.pitch, d.img.row_bytes, r1 - r0,
+                               cudaMemcpyDeviceToHost, ctx->stream);
+      else
+        ce = cudaMemcpyAsync(d.stage + r0 * d.pitch, d.dev + r0 * d.pitch, (r1 - r0) * d.pitch,
+                             cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    if (ce == cudaSuccess) ce = cudaEventRecord(events[t], ctx->stream);
+    if (ce != cudaSuccess) {
+      events.resize(t + (events[t] ? 1 : 0));
+      return finish(cuda_fail(ctx, ce));
+    }
+  }
+  if (!d.pinned) {
+    Transfer x{ctx, &d, &events};
+    e = mt.parallel(download_task, &x, mt.parallel_data, d.tasks);
+    if (e != KLEIDICV_OK) return finish(e);
+  }
+  return finish(KLEIDICV_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
+kleidicv_error_t kleidicv_gpu_thread_pool_create(kleidicv_gpu_thread_pool_t **pool,
+                                                 unsigned threads) {
+  if (!pool) return KLEIDICV_ERROR_NULL_POINTER;
+  if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
+  auto *p = new kleidicv_gpu_thread_pool();
+  for (unsigned i = 1; i < threads; ++i) p->workers.emplace_back([p] { p->worker(); });
+  *pool = p;
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t kleidicv_gpu_thread_pool_destroy(kleidicv_gpu_thread_pool_t *pool) {
+  if (!pool) return KLEIDICV_ERROR_NULL_POINTER;
+  {
+    std::lock_guard<std::mutex> l(pool->m);
+    pool->stop = true;
+  }
+  pool->wake.notify_all();
+  for (auto &t : pool->workers) t.join();
+  delete pool;
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t kleidicv_gpu_thread_pool_parallel(kleidicv_thread_callback callback,
+                                                   void *callback_data, void *parallel_data,
+                                                   unsigned task_count) {
+  auto *p = static_cast<kleidicv_gpu_thread_pool *>(parallel_data);
+  if (!p || !callback) return KLEIDICV_ERROR_NULL_POINTER;
+  if (task_count == 0) return KLEIDICV_OK;
+  std::lock_guard<std::mutex> one_call(p->call);
+  kleidicv_gpu_thread_pool::Job j{callback, callback_data, task_count};
+  {
+    std::lock_guard<std::mutex> l(p->m);
+    p->job = j;
+    p->next = 0;
+    p->error = KLEIDICV_OK;
+    p->finished = 0;
+    ++p->generation;
+  }
+  p->wake.notify_all();
+  p->run(j);
+  std::unique_lock<std::mutex> l(p->m);
+  p->done.wait(l, [&] { return p->finished == p->workers.size(); });
+  return static_cast<kleidicv_error_t>(p->error.load());
+}
+
+kleidicv_error_t kleidicv_gpu_thread_gaussian_blur_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height, float sigma_x,
+    float sigma_y, kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt) {
+  Prepared p;
+  const kleidicv_error_t v =
+      kcv::prepare_gaussian(src, src_stride, dst, dst_stride, width, height, channels,
+                            kernel_width, kernel_height, sigma_x, sigma_y, border_type, false, 0,
+                            &p);
+  const size_t rb = width * channels;
+  return run_threaded(
+      v, p, {src, src_stride, rb, height}, {dst, dst_stride, rb, height},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_gaussian_blur_u8(static_cast<const uint8_t *>(s), ss,
+                                             static_cast<uint8_t *>(d), ds, width, height, channels,
+                                             kernel_width, kernel_height, sigma_x, sigma_y,
+                                             border_type, c);
+      },
+      mt);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint8_t *kernel_x, size_t kernel_width,
+    const uint8_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_separable(1, src, src_stride, dst, dst_stride, width,
+                                                    height, channels, kernel_x, kernel_width,
+                                                    kernel_y, kernel_height, border_type, false,
+                                                    0, &p);
+  const size_t rb = width * channels;
+  return run_threaded(
+      v, p, {src, src_stride, rb, height}, {dst, dst_stride, rb, height},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_separable_filter_2d_u8(static_cast<const uint8_t *>(s), ss,
+                                                   static_cast<uint8_t *>(d), ds, width, height,
+                                                   channels, kernel_x, kernel_width, kernel_y,
+                                                   kernel_height, border_type, c);
+      },
+      mt);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u16(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint16_t *kernel_x, size_t kernel_width,
+    const uint16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_separable(2, src, src_stride, dst, dst_stride, width,
+                                                    height, channels, kernel_x, kernel_width,
+                                                    kernel_y, kernel_height, border_type, false,
+                                                    0, &p);
+  const size_t rb = width * channels * 2;
+  return run_threaded(
+      v, p, {reinterpret_cast<const uint8_t *>(src), src_stride, rb, height},
+      {reinterpret_cast<const uint8_t *>(dst), dst_stride, rb, height},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_separable_filter_2d_u16(static_cast<const uint16_t *>(s), ss,
+                                                    static_cast<uint16_t *>(d), ds, width, height,
+                                                    channels, kernel_x, kernel_width, kernel_y,
+                                                    kernel_height, border_type, c);
+      },
+      mt);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_blur_and_downsample_u8(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height, uint8_t *dst,
+    size_t dst_stride, size_t channels, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_blurdown(src, src_stride, src_width, src_height, dst,
+                                                   dst_stride, channels, border_type, false, 0, &p);
+  return run_threaded(
+      v, p, {src, src_stride, src_width * channels, src_height},
+      {dst, dst_stride, (src_width + 1) / 2 * channels, (src_height + 1) / 2},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_blur_and_downsample_u8(static_cast<const uint8_t *>(s), ss, src_width,
+                                                   src_height, static_cast<uint8_t *>(d), ds,
+                                                   channels, border_type, c);
+      },
+      mt);
+}
+
+static kleidicv_error_t thread_sobel(bool horizontal, const uint8_t *src, size_t src_stride,
+                                     int16_t *dst, size_t dst_stride, size_t width,
+                                     size_t height, size_t channels,
+                                     kleidicv_thread_multithreading mt) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_sobel(horizontal, src, src_stride, dst, dst_stride,
+                                                width, height, channels, &p);
+  return run_threaded(
+      v, p, {src, src_stride, width * channels, height},
+      {reinterpret_cast<const uint8_t *>(dst), dst_stride, 2 * width * channels, height},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        const uint8_t *su = static_cast<const uint8_t *>(s);
+        int16_t *di = static_cast<int16_t *>(d);
+        return horizontal
+                   ? kleidicv_gpu_sobel_3x3_horizontal_s16_u8(su, ss, di, ds, width, height,
+                                                              channels, c)
+                   : kleidicv_gpu_sobel_3x3_vertical_s16_u8(su, ss, di, ds, width, height,
+                                                            channels, c);
+      },
+      mt);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, kleidicv_thread_multithreading mt) {
+  return thread_sobel(true, src, src_stride, dst, dst_stride, width, height, channels, mt);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, kleidicv_thread_multithreading mt) {
+  return thread_sobel(false, src, src_stride, dst, dst_stride, width, height, channels, mt);
+}
+
+}  // extern "C"
