@@ -62,7 +62,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,thread_api,serving",
+    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,median,thread_api,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
     ap.add_argument("--serving-seconds", type=float, default=3.0)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
@@ -561,6 +561,39 @@ def section_thread_api(torch, kcv, cores):
     return out
 
 
+def section_median(torch, kcv, ctx, stream):
+    """Median blur, 1920x1080 (seed 6): u8 1 and 3 channels with K = 3, 5, 7
+    (selection per element) and K = 15 (sliding histograms), f32 1 channel
+    with K = 5; per-call time and bit-exactness on 16 rows against the
+    oracle."""
+    from oracle import oracle
+
+    w, h = 1920, 1080
+    rng = np.random.default_rng(6)
+    out = {"config": "1920x1080, REPLICATE, seed 6; CUDA events over 20 calls"}
+    for dtype, c, k in (("u8", 1, 3), ("u8", 1, 5), ("u8", 1, 7), ("u8", 3, 5), ("u8", 1, 15), ("f32", 1, 5)):
+        dt = oracle.MEDIAN_DTYPES[dtype]
+        host = rng.integers(0, 256, (h, w * c)).astype(dt)
+        src = torch.from_numpy(host).cuda()
+        dst = torch.empty_like(src)
+        es = host.itemsize
+
+        def call(i):
+            e = kcv.median_blur(dtype, src.data_ptr(), w * c * es, dst.data_ptr(), w * c * es, w, h, c, k, k,
+                                kcv.REPLICATE, ctx)
+            assert e == kcv.OK, e
+
+        call(0)
+        ms = _events_time(torch, stream, call, 20)
+        rows = list(range(0, h, h // 16))[:16]
+        exact = bool(np.array_equal(dst.cpu().numpy()[rows],
+                                    oracle.median_blur(host, w, h, c, k, kcv.REPLICATE, out_rows=rows)))
+        out[f"{dtype}_c{c}_k{k}"] = {"us_per_call": round(ms * 1e3, 1),
+                                     "mpix_s": round(w * h / (ms * 1e-3) / 1e6, 1), "bit_exact_rows": exact}
+        del src, dst
+    return out
+
+
 def _log_uniform(rng, lo, hi):
     return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
 
@@ -882,6 +915,8 @@ def run_sections(args, names):
                 out[name] = section_batched(torch, kcv, ctx, stream, cores)
             elif name == "pyramid":
                 out[name] = section_pyramid(torch, kcv, ctx, stream)
+            elif name == "median":
+                out[name] = section_median(torch, kcv, ctx, stream)
             elif name == "thread_api":
                 out[name] = section_thread_api(torch, kcv, cores)
             elif name == "sobel":

@@ -33,6 +33,9 @@
  *  kleidicv_gpu_sobel_3x3_vertical_s16_u8
  *                                        kleidicv/include/kleidicv/kleidicv.h:2006-2008
  *                                        (kleidicv/src/filters/sobel_api.cpp:53-58)
+ *  kleidicv_gpu_median_blur_{s8,u8,u16,s16,u32,s32,f32}
+ *                                        kleidicv/include/kleidicv/kleidicv.h:2225-2302
+ *                                        (kleidicv/src/filters/median_blur_api.cpp:42-242)
  * and, with the same argument lists, the threaded variants
  *  kleidicv_thread_{gaussian_blur_u8,separable_filter_2d_u8,
  *  separable_filter_2d_u16,blur_and_downsample_u8}
@@ -154,6 +157,41 @@ kleidicv_error_t kleidicv_gpu_sobel_3x3_horizontal_s16_u8(
 kleidicv_error_t kleidicv_gpu_sobel_3x3_vertical_s16_u8(
     const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
     size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
+
+/* Median blur of the K x K window (kleidicv.h:2225-2302; validation
+ * kleidicv/include/kleidicv/filters/median_blur.h:148-193): K odd, 3..7 for
+ * every type, 3..255 for u8; REPLICATE, REFLECT, WRAP or REVERSE; width and
+ * height >= K - 1; src != dst.  The median of the window is unique, so the
+ * results equal the reference's sorting networks and histograms (f32: for
+ * inputs without NaN; -0.0 orders below +0.0). */
+kleidicv_error_t kleidicv_gpu_median_blur_s8(
+    const int8_t *src, size_t src_stride, int8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_u16(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_s16(
+    const int16_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_u32(
+    const uint32_t *src, size_t src_stride, uint32_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_s32(
+    const int32_t *src, size_t src_stride, int32_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_median_blur_f32(
+    const float *src, size_t src_stride, float *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
 
 /* ------------------------------------------------------------------------ */
 /* Extensions (no reference counterpart; semantics defined by this library,

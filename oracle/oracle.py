@@ -145,6 +145,57 @@ def sobel_3x3_s16_u8(src, width, height, channels, horizontal, *, nthreads=1, ds
     return err, dst
 
 
+# --- median blur (kleidicv/src/filters/median_blur_api.cpp, filters/median_blur.h:148-193)
+
+MEDIAN_DTYPES = {"s8": np.int8, "u8": np.uint8, "u16": np.uint16, "s16": np.int16, "u32": np.uint32,
+                 "s32": np.int32, "f32": np.float32}
+
+
+def median_blur_check(dtype, src_null, src_stride, dst_null, dst_stride, width, height, channels, kw, kh,
+                      border, same_buffer=False):
+    """Error code of kleidicv_median_blur_<dtype>, in the reference's order:
+    pointers and strides, image size, then the NOT_IMPLEMENTED conditions."""
+    es = np.dtype(MEDIAN_DTYPES[dtype]).itemsize
+    if src_null:
+        return NULL_POINTER
+    if height > 1 and src_stride % es:
+        return ALIGNMENT
+    if dst_null:
+        return NULL_POINTER
+    if height > 1 and dst_stride % es:
+        return ALIGNMENT
+    if width * height > (1 << 48) - 1:
+        return RANGE
+    kmax = 255 if dtype == "u8" else 7
+    ok = (not same_buffer and channels <= 4 and height >= kh - 1 and width >= kw - 1 and kw == kh
+          and 3 <= kw <= kmax and kw % 2 == 1 and border in (1, 2, 3, 4))
+    return OK if ok else NOT_IMPLEMENTED
+
+
+def median_blur(src, width, height, channels, ksize, border, out_rows=None):
+    """The reference test's model (test/api/test_median_blur.cpp:108-186): for
+    every element, sort the border-mapped K x K window (same channel) and take
+    the middle value.  `src` is 2-D (rows x elements, any padding).  With
+    `out_rows` only those destination rows are computed (in that order)."""
+    r = ksize // 2
+    rows = np.array([border_map(i, height, border) for i in range(-r, height + r)])
+    cols = np.array([border_map(i, width, border) for i in range(-r, width + r)])
+    img = np.asarray(src)[:height, : width * channels].reshape(height, width, channels)
+    padded = img[rows][:, cols]  # (h + 2r, w + 2r, c)
+    mid = (ksize * ksize) // 2
+    want = list(range(height)) if out_rows is None else list(out_rows)
+    out = np.empty((len(want), width, channels), img.dtype)
+    # Rows in chunks of at most ~32 M window elements.
+    step = max(1, (32 << 20) // max(1, width * channels * ksize * ksize))
+    for i in range(0, len(want), step):
+        chunk = want[i:i + step]
+        win = np.stack([np.lib.stride_tricks.sliding_window_view(padded[y:y + ksize], (ksize, ksize),
+                                                                 axis=(0, 1))[0] for y in chunk])
+        flat = win.reshape(len(chunk), width, channels, ksize * ksize)
+        out[i:i + len(chunk)] = np.partition(flat, mid, axis=-1)[..., mid]
+    return out.reshape(len(want), width * channels)
+
+
 # --- LK optical-flow pyramid (kleidicv/include/kleidicv/analysis/build_optical_flow_pyr_lk_pyramid.h)
 
 MAX_LK_WINDOW = 2047  # KLEIDICV_MAX_OPTICAL_FLOW_PYR_LK_WINDOW_SIZE, kleidicv.h:119

@@ -86,6 +86,8 @@ SIGNATURES = {
     "kleidicv_gpu_blur_and_downsample_u8_ex": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, _u8, _vp]),
     "kleidicv_gpu_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
     "kleidicv_gpu_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp]),
+    **{f"kleidicv_gpu_median_blur_{t}": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _i, _vp])
+       for t in ("s8", "u8", "u16", "s16", "u32", "s32", "f32")},
     # Threaded API (include/kleidicv_gpu_thread.h): host images, the caller's scheduler.
     "kleidicv_gpu_thread_gaussian_blur_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f, _i,
                                                   ThreadMT]),
@@ -280,6 +282,19 @@ def blur_and_downsample_u8(src, src_stride, src_width, src_height, dst, dst_stri
     return lib().kleidicv_gpu_blur_and_downsample_u8_ex(src, src_stride, src_width, src_height, dst,
                                                         dst_stride, channels, border_type,
                                                         border_value, _h(ctx))
+
+
+MEDIAN_TYPES = {"s8": "int8", "u8": "uint8", "u16": "uint16", "s16": "int16", "u32": "uint32", "s32": "int32",
+                "f32": "float32"}
+
+
+def median_blur(dtype, src, src_stride, dst, dst_stride, width, height, channels, kernel_width, kernel_height,
+                border_type, ctx=None):
+    """kleidicv_median_blur_<dtype> (kleidicv/src/filters/median_blur_api.cpp:42-242);
+    dtype in s8, u8, u16, s16, u32, s32, f32."""
+    fn = getattr(lib(), f"kleidicv_gpu_median_blur_{dtype}")
+    return fn(src, src_stride, dst, dst_stride, width, height, channels, kernel_width, kernel_height, border_type,
+              _h(ctx))
 
 
 THREAD_CALLBACK = ctypes.CFUNCTYPE(_i, ctypes.c_uint, ctypes.c_uint, _vp)

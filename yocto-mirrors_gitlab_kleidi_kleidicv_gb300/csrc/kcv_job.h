@@ -127,4 +127,22 @@ struct GenericJob {
   uint8_t half[128];       // half kernel, half[ksize/2] is the centre weight
 };
 
+// Median blur (csrc/median.cu): element type, window size K, border.
+enum MedianElem : int32_t {
+  MEDIAN_S8 = 0,
+  MEDIAN_U8,
+  MEDIAN_U16,
+  MEDIAN_S16,
+  MEDIAN_U32,
+  MEDIAN_S32,
+  MEDIAN_F32,
+};
+
+struct MedianJob {
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride, dst_stride;  // bytes
+  int32_t width, height, channels, ksize, border, elem;
+};
+
 }  // namespace kcv

@@ -67,4 +67,8 @@ cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch,
 // so that later launches do not trigger CUDA's lazy module loading.
 cudaError_t preload_generic_gaussian();
 
+// Median blur: K in {3, 5, 7} for every element type (selection per
+// element), K in 9..255 odd for u8 (sliding histograms).
+cudaError_t launch_median(const MedianJob &job, cudaStream_t stream);
+
 }  // namespace kcv
