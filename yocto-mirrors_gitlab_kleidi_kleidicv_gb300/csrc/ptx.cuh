@@ -144,4 +144,11 @@ __device__ __forceinline__ void st_v4(void *p, uint4 v) {
                : "memory");
 }
 
+// One 32-byte store (sm_100+); the address must be 32-byte aligned.
+__device__ __forceinline__ void st_v8(void *p, uint4 lo, uint4 hi) {
+  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(lo.x),
+               "r"(lo.y), "r"(lo.z), "r"(lo.w), "r"(hi.x), "r"(hi.y), "r"(hi.z), "r"(hi.w)
+               : "memory");
+}
+
 }  // namespace kcv

@@ -419,20 +419,27 @@ __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const u
 //   X: V[x + C] - V[x - C] of the [1 2 1] vertical sums (sobel_neon.cpp:55-60);
 //   Y: V[x - C] + 2 V[x] + V[x + C] of the +256-biased [-1 0 1] vertical
 //      differences (sobel_neon.cpp:111-118), bias 4 * 256 removed.
+//
+// A 3-tap filter over at most 4 channels reaches one 32-bit word past the
+// lane's own four in each of its two lane arrays, so the neighbours' edge
+// words come by warp shuffle straight from registers (`v` = lo words 0..3,
+// hi words 4..7 of the lane's vertical results); lanes 0 and 31 are halo
+// lanes whose results are discarded.
 template <int MODE, int C>
-__device__ __forceinline__ void horizontal_sobel(const uint32_t *vlo_s, const uint32_t *vhi_s,
-                                                 int tid, uint4 &o0, uint4 &o1) {
+__device__ __forceinline__ void horizontal_sobel(const uint32_t (&v)[8], uint4 &o0, uint4 &o1) {
   using G = Geo<MODE, 3, C>;
   constexpr int HW = G::HW, NW = G::NW;
+  static_assert(HW == 4, "one halo chunk per side");
   uint32_t lo[NW], hi[NW];
-  const int base = 4 * tid - HW;
 #pragma unroll
-  for (int k = 0; k < NW; k += 4) {
-    const uint4 a = *reinterpret_cast<const uint4 *>(vlo_s + base + k);
-    const uint4 b = *reinterpret_cast<const uint4 *>(vhi_s + base + k);
-    lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
-    hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
+  for (int k = 0; k < 4; ++k) {
+    lo[HW + k] = v[k];
+    hi[HW + k] = v[4 + k];
   }
+  lo[HW - 1] = __shfl_up_sync(0xffffffffu, v[3], 1);
+  hi[HW - 1] = __shfl_up_sync(0xffffffffu, v[7], 1);
+  lo[HW + 4] = __shfl_down_sync(0xffffffffu, v[0], 1);
+  hi[HW + 4] = __shfl_down_sync(0xffffffffu, v[4], 1);
   uint32_t acc[8];
   static_for<0, 8>([&](auto jc) {
     constexpr int J = decltype(jc)::value;
@@ -784,6 +791,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // Destination rows all start 16-byte aligned when base and stride are.
   const bool dst_rows_aligned =
       ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 15) == 0;
+  // Sobel chunks are 32 destination bytes: one 32-byte store when rows allow.
+  const bool dst_rows_aligned32 =
+      ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 31) == 0;
   // This lane writes a whole 16-byte chunk with one vector store.
   const bool stores = emits && active && xb < wcb;
   const bool full_store = stores && dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
@@ -974,7 +984,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     static_for<0, M>([&](auto mc) {
       constexpr int Mi = decltype(mc)::value;
       uint32_t *vb = vwarp + (Mi & 1) * (kVRowBytes / 4);
-      if constexpr (ModeTraits<MODE>::LANES) {
+      if constexpr (ModeTraits<MODE>::SOBEL) {
+        // No V row: the neighbours' words come by shuffle (horizontal_sobel).
+      } else if constexpr (ModeTraits<MODE>::LANES) {
         *reinterpret_cast<uint4 *>(vb + 4 * lane) = make_uint4(v[Mi][0], v[Mi][1], v[Mi][2], v[Mi][3]);
         *reinterpret_cast<uint4 *>(vb + 128 + 4 * lane) =
             make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
@@ -983,7 +995,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         *reinterpret_cast<uint4 *>(vb + 8 * lane + 4) =
             make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
       }
-      __syncwarp();
+      if constexpr (!ModeTraits<MODE>::SOBEL) __syncwarp();
       if constexpr (MODE == MODE_BLURDOWN) {
         uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + Mi) * dst_stride;
         if (Mi < mcount) {
@@ -1006,12 +1018,16 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
       } else if constexpr (ModeTraits<MODE>::SOBEL) {
         // 32 destination bytes per chunk (s16 per source byte).
         uint4 r0, r1;
-        horizontal_sobel<MODE, C>(vb, vb + 128, hlane, r0, r1);
+        horizontal_sobel<MODE, C>(v[Mi], r0, r1);
         uint8_t *drow = dblock + Mi * dst_stride;
         const bool row_ok = Mi < mcount;
         if (full_store && row_ok) {
-          *reinterpret_cast<uint4 *>(drow) = r0;
-          *reinterpret_cast<uint4 *>(drow + 16) = r1;
+          if (dst_rows_aligned32) {
+            st_v8(drow, r0, r1);
+          } else {
+            *reinterpret_cast<uint4 *>(drow) = r0;
+            *reinterpret_cast<uint4 *>(drow + 16) = r1;
+          }
         }
         if (partial_store && row_ok) {
           const uint32_t w8[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
