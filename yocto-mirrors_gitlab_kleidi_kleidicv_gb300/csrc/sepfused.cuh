@@ -325,21 +325,88 @@ __device__ __forceinline__ uint32_t pair_at(const uint32_t (&lo)[NW], const uint
   }
 }
 
+// The words of a lane array that the lane-form horizontal pass reads,
+// relative to the lane's own first word: [first(), last()] (pair_at's word
+// w - HW, plus w + 1 - HW for pairs straddling two words).
+template <int K, int C>
+struct LaneSpan {
+  static constexpr int first() {
+    int m = 0;
+    for (int d = -(K / 2); d <= K / 2; ++d)
+      for (int p = 0; p < 2; ++p) m = floor_div(p + d * C, 4) < m ? floor_div(p + d * C, 4) : m;
+    return m;
+  }
+  static constexpr int last() {
+    int m = 3;
+    for (int d = -(K / 2); d <= K / 2; ++d)
+      for (int p = 0; p < 2; ++p) {
+        const int g = p + d * C, q = floor_div(g, 4), w = 3 + q + (g - 4 * q >= 2 ? 1 : 0);
+        m = w > m ? w : m;
+      }
+    return m;
+  }
+  // Words fetched from neighbouring lanes, per array.
+  static constexpr int neighbour_words = (last() - 3) - first();
+};
+
+// Lane-form modes whose horizontal pass takes the neighbours' words by warp
+// shuffle from registers instead of through the warp's shared V row: those
+// that need at most kShuffleWords neighbour words per lane array.
+#ifndef KCV_SHUFFLE_WORDS
+#define KCV_SHUFFLE_WORDS 6
+#endif
+template <int MODE, int K, int C>
+constexpr bool shuffle_horizontal() {
+  return ModeTraits<MODE>::LANES && MODE != MODE_BLURDOWN && !ModeTraits<MODE>::SOBEL &&
+         LaneSpan<K, C>::neighbour_words <= KCV_SHUFFLE_WORDS;
+}
+
+// Fills the words of lo/hi that the horizontal pass reads from the lane's
+// vertical results `v` (lo words 0..3, hi words 4..7) and its neighbours'.
+// Halo lanes (whose results are discarded) may receive wrapped values.
+template <int MODE, int K, int C, int NW>
+__device__ __forceinline__ void lanes_from_registers(const uint32_t (&v)[8], uint32_t (&lo)[NW],
+                                                     uint32_t (&hi)[NW]) {
+  using G = Geo<MODE, K, C>;
+  constexpr int HW = G::HW;
+  static_for<LaneSpan<K, C>::first(), LaneSpan<K, C>::last() + 1>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    constexpr int delta = floor_div(k, 4), word = k - 4 * delta;
+    static_assert(HW + k >= 0 && HW + k < NW, "word outside the lane arrays");
+    static_assert(delta >= -G::HC && delta <= G::HC, "neighbour beyond the halo lanes");
+    if constexpr (delta == 0) {
+      lo[HW + k] = v[word];
+      hi[HW + k] = v[4 + word];
+    } else if constexpr (delta < 0) {
+      lo[HW + k] = __shfl_up_sync(0xffffffffu, v[word], -delta);
+      hi[HW + k] = __shfl_up_sync(0xffffffffu, v[4 + word], -delta);
+    } else {
+      lo[HW + k] = __shfl_down_sync(0xffffffffu, v[word], delta);
+      hi[HW + k] = __shfl_down_sync(0xffffffffu, v[4 + word], delta);
+    }
+  });
+}
+
 // The 16 output bytes of the thread for the lane-form modes.  The V row
-// holds, per lane, its lo words then (128 words later) its hi words.
-template <int MODE, int K, int C, bool NARROW>
+// holds, per lane, its lo words then (128 words later) its hi words; with
+// REGS the words come from `v` and the neighbours' registers instead.
+template <int MODE, int K, int C, bool NARROW, bool REGS = false>
 __device__ __forceinline__ uint4 horizontal_lanes(const uint32_t *vlo_s, const uint32_t *vhi_s,
-                                                  int tid, const Taps &tp) {
+                                                  int tid, const uint32_t (&v)[8], const Taps &tp) {
   using G = Geo<MODE, K, C>;
   constexpr int R = K / 2, HW = G::HW, NW = G::NW;
   uint32_t lo[NW], hi[NW];
-  const int base = 4 * tid - HW;
+  if constexpr (REGS) {
+    lanes_from_registers<MODE, K, C, NW>(v, lo, hi);
+  } else {
+    const int base = 4 * tid - HW;
 #pragma unroll
-  for (int k = 0; k < NW; k += 4) {
-    const uint4 a = *reinterpret_cast<const uint4 *>(vlo_s + base + k);
-    const uint4 b = *reinterpret_cast<const uint4 *>(vhi_s + base + k);
-    lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
-    hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
+    for (int k = 0; k < NW; k += 4) {
+      const uint4 a = *reinterpret_cast<const uint4 *>(vlo_s + base + k);
+      const uint4 b = *reinterpret_cast<const uint4 *>(vhi_s + base + k);
+      lo[k] = a.x; lo[k + 1] = a.y; lo[k + 2] = a.z; lo[k + 3] = a.w;
+      hi[k] = b.x; hi[k + 1] = b.y; hi[k + 2] = b.z; hi[k + 3] = b.w;
+    }
   }
   // Taps outer, the eight lane pairs (J = 2*I + P) inner.
   uint32_t acc[8];
@@ -984,8 +1051,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
     static_for<0, M>([&](auto mc) {
       constexpr int Mi = decltype(mc)::value;
       uint32_t *vb = vwarp + (Mi & 1) * (kVRowBytes / 4);
-      if constexpr (ModeTraits<MODE>::SOBEL) {
-        // No V row: the neighbours' words come by shuffle (horizontal_sobel).
+      constexpr bool kRegs = shuffle_horizontal<MODE, K, C>();
+      if constexpr (ModeTraits<MODE>::SOBEL || kRegs) {
+        // No V row: the neighbours' words come by shuffle.
       } else if constexpr (ModeTraits<MODE>::LANES) {
         *reinterpret_cast<uint4 *>(vb + 4 * lane) = make_uint4(v[Mi][0], v[Mi][1], v[Mi][2], v[Mi][3]);
         *reinterpret_cast<uint4 *>(vb + 128 + 4 * lane) =
@@ -995,7 +1063,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         *reinterpret_cast<uint4 *>(vb + 8 * lane + 4) =
             make_uint4(v[Mi][4], v[Mi][5], v[Mi][6], v[Mi][7]);
       }
-      if constexpr (!ModeTraits<MODE>::SOBEL) __syncwarp();
+      if constexpr (!ModeTraits<MODE>::SOBEL && !kRegs) __syncwarp();
       if constexpr (MODE == MODE_BLURDOWN) {
         uint8_t *drow = dst_base + static_cast<int64_t>(oy0 + ob + Mi) * dst_stride;
         if (Mi < mcount) {
@@ -1042,7 +1110,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         // of the band are not stored.
         uint4 r;
         if constexpr (ModeTraits<MODE>::LANES)
-          r = horizontal_lanes<MODE, K, C, NARROW>(vb, vb + 128, hlane, tp);
+          r = horizontal_lanes<MODE, K, C, NARROW, kRegs>(vb, vb + 128, hlane, v[Mi], tp);
         else
           r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
         uint8_t *drow = dblock + Mi * dst_stride;
