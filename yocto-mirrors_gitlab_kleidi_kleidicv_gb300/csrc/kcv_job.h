@@ -100,18 +100,6 @@ struct BatchTile {
   uint16_t strip, band;
 };
 
-// Batched kernel families (one persistent kernel each, grouped by register
-// class): generated-sigma sizes 3..9, sigma 15/21, binomial, separable,
-// blur-and-downsample.
-enum BatchFamilyId : int32_t {
-  BFAM_SIGMA_SMALL = 0,
-  BFAM_SIGMA_LARGE = 1,
-  BFAM_BINOM = 2,
-  BFAM_SEP = 3,
-  BFAM_BLURDOWN = 4,
-  BFAM_COUNT = 5,
-};
-
 // Generic per-element Gaussian (any odd size up to 255).
 struct GenericJob {
   const uint8_t *src;
