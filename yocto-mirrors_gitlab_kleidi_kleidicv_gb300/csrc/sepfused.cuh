@@ -357,8 +357,9 @@ struct LaneSpan {
 #endif
 template <int MODE, int K, int C>
 constexpr bool shuffle_horizontal() {
-  return ModeTraits<MODE>::LANES && MODE != MODE_BLURDOWN && !ModeTraits<MODE>::SOBEL &&
-         LaneSpan<K, C>::neighbour_words <= KCV_SHUFFLE_WORDS;
+  if constexpr (MODE == MODE_BLURDOWN || ModeTraits<MODE>::SOBEL) return false;
+  else if constexpr (ModeTraits<MODE>::LANES) return LaneSpan<K, C>::neighbour_words <= KCV_SHUFFLE_WORDS;
+  else return 2 * (K / 2) * C <= KCV_SHUFFLE_WORDS;  // u16/s16: one 32-bit word per element
 }
 
 // Fills the words of lo/hi that the horizontal pass reads from the lane's
@@ -532,16 +533,30 @@ __device__ __forceinline__ void horizontal_sobel(const uint32_t (&v)[8], uint4 &
 
 // u16 / s16 separable: the V row holds 8 32-bit elements per lane (u16
 // values clamped to 65535, or s16 vertical sums), lane-major.
-template <int MODE, int K, int C, bool NARROW>
-__device__ __forceinline__ uint4 horizontal_wide(const uint32_t *v_s, int tid, const Taps &tp) {
+template <int MODE, int K, int C, bool NARROW, bool REGS = false>
+__device__ __forceinline__ uint4 horizontal_wide(const uint32_t *v_s, int tid,
+                                                 const uint32_t (&own)[8], const Taps &tp) {
   using G = Geo<MODE, K, C>;
   constexpr int R = K / 2, HE = 2 * G::HW, NE = 8 + 2 * HE;  // elements
   uint32_t v[NE];
-  const int base = 8 * tid - HE;
+  if constexpr (REGS) {
+    // Elements -R*C .. 7+R*C around the lane's own eight: the neighbours'
+    // come by shuffle (halo lanes, whose results are discarded, may wrap).
+    static_for<-R * C, 8 + R * C>([&](auto ec) {
+      constexpr int e = decltype(ec)::value;
+      constexpr int delta = floor_div(e, 8), idx = e - 8 * delta;
+      static_assert(delta >= -G::HC && delta <= G::HC, "neighbour beyond the halo lanes");
+      if constexpr (delta == 0) v[HE + e] = own[idx];
+      else if constexpr (delta < 0) v[HE + e] = __shfl_up_sync(0xffffffffu, own[idx], -delta);
+      else v[HE + e] = __shfl_down_sync(0xffffffffu, own[idx], delta);
+    });
+  } else {
+    const int base = 8 * tid - HE;
 #pragma unroll
-  for (int k = 0; k < NE; k += 4) {
-    const uint4 a = *reinterpret_cast<const uint4 *>(v_s + base + k);
-    v[k] = a.x; v[k + 1] = a.y; v[k + 2] = a.z; v[k + 3] = a.w;
+    for (int k = 0; k < NE; k += 4) {
+      const uint4 a = *reinterpret_cast<const uint4 *>(v_s + base + k);
+      v[k] = a.x; v[k + 1] = a.y; v[k + 2] = a.z; v[k + 3] = a.w;
+    }
   }
   uint32_t o[8];
   if constexpr (MODE == MODE_SEP_U16) {
@@ -1112,7 +1127,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         if constexpr (ModeTraits<MODE>::LANES)
           r = horizontal_lanes<MODE, K, C, NARROW, kRegs>(vb, vb + 128, hlane, v[Mi], tp);
         else
-          r = horizontal_wide<MODE, K, C, NARROW>(vb, hlane, tp);
+          r = horizontal_wide<MODE, K, C, NARROW, kRegs>(vb, hlane, v[Mi], tp);
         uint8_t *drow = dblock + Mi * dst_stride;
         const bool row_ok = Mi < mcount;
         if (full_store && row_ok) *reinterpret_cast<uint4 *>(drow) = r;
