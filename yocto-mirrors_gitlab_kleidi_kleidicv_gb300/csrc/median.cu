@@ -12,11 +12,11 @@
 //    compare-exchange passes, drop both (neither can be the median: equal
 //    numbers are dropped below and above it) and take in the next value;
 //    the last three hold the median.
-//  * u8, K >= 9: Huang's sliding histogram.  A thread owns a run of pixels of
-//    one row and channel and a 256-bin histogram in shared memory (bins
-//    outermost, so the 64 threads of a block hit distinct banks); moving one
-//    pixel right removes a column, adds a column and moves the median bin by
-//    the count of values that crossed it.
+//  * u8, K >= 9: Huang's sliding histogram.  A thread owns a run of
+//    max(16, K/2) pixels of one row and channel and a 256-bin histogram in
+//    shared memory (bins outermost, so the 64 threads of a block hit distinct
+//    banks); moving one pixel right removes a column, adds a column and moves
+//    the median bin by the count of values that crossed it.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -129,22 +129,26 @@ __global__ void __launch_bounds__(128) median_small_kernel(const uint8_t *src, i
 }
 
 constexpr int kHistThreads = 64;
-constexpr int kHistRun = 64;  // pixels per thread
+
+// Pixels per thread: at least K/2, so that the O(K^2) start costs no more per
+// pixel than the O(K) steps, and otherwise short, so that a 1080p image still
+// gives tens of thousands of threads.
+int hist_run(int k) { return std::max(16, (k / 2 + 15) / 16 * 16); }
 
 __global__ void __launch_bounds__(kHistThreads) median_hist_kernel(const uint8_t *src,
                                                                   int64_t src_stride,
                                                                   uint8_t *dst,
                                                                   int64_t dst_stride, int w,
                                                                   int h, int c, int k,
-                                                                  int border) {
+                                                                  int border, int run) {
   __shared__ uint16_t hist[256 * kHistThreads];  // [bin][thread]; counts <= 255 * 255
   const int tid = threadIdx.x;
   const int g = blockIdx.x * kHistThreads + tid;  // (segment, channel) item of row y
   const int y = blockIdx.y;
   const int ch = g % c, seg = g / c;
-  const int x0 = seg * kHistRun;
+  const int x0 = seg * run;
   if (x0 >= w) return;  // no __syncthreads below: threads are independent
-  const int x1 = min(w, x0 + kHistRun);
+  const int x1 = min(w, x0 + run);
   const int r = k / 2;
   const int m = (k * k - 1) / 2;  // rank of the median
   for (int b = 0; b < 256; ++b) hist[b * kHistThreads + tid] = 0;
@@ -197,12 +201,13 @@ cudaError_t launch_typed(const MedianJob &j, cudaStream_t s) {
 cudaError_t launch_median(const MedianJob &j, cudaStream_t s) {
   if (j.ksize > 7) {
     if (j.elem != MEDIAN_U8) return cudaErrorInvalidValue;
-    const int items = j.channels * ((j.width + kHistRun - 1) / kHistRun);
+    const int run = hist_run(j.ksize);
+    const int items = j.channels * ((j.width + run - 1) / run);
     dim3 grid(static_cast<unsigned>((items + kHistThreads - 1) / kHistThreads),
               static_cast<unsigned>(j.height));
     median_hist_kernel<<<grid, kHistThreads, 0, s>>>(j.src, j.src_stride, j.dst, j.dst_stride,
                                                      j.width, j.height, j.channels, j.ksize,
-                                                     j.border);
+                                                     j.border, run);
     return cudaGetLastError();
   }
   switch (j.elem) {
