@@ -69,12 +69,14 @@ struct Image {
 // pitch), then waits for the result.  `validation` is the entry's own check
 // with the caller's pointers (`p` its outcome): nothing is copied for a call
 // it rejects or that has nothing to compute.
-int run_staged(kleidicv_error_t validation, const kcv::Prepared &p, const Image &src,
-               const Image &dst,
+int run_staged(kleidicv_error_t validation, const kcv::Prepared &p, Image src, Image dst,
                const std::function<kleidicv_error_t(const void *, size_t, void *, size_t,
                                                     kleidicv_gpu_context_t *)> &op) {
   if (validation != KLEIDICV_OK) return convert_error(validation);
   if (p.kind == kcv::Prepared::NOTHING) return kHalOk;
+  // A single-row image may come with any stride (the reference ignores it).
+  if (src.rows <= 1) src.step = src.row_bytes;
+  if (dst.rows <= 1) dst.step = dst.row_bytes;
   kleidicv_gpu_context_t *ctx = nullptr;
   kleidicv_error_t e = kcv::resolve_context(ctx);
   if (e != KLEIDICV_OK) return convert_error(e);

@@ -190,6 +190,9 @@ kleidicv_error_t run_threaded(kleidicv_error_t validation, const Prepared &p, Ho
   Side s, d;
   s.img = src;
   d.img = dst;
+  // A single-row image may come with any stride (the reference ignores it).
+  for (Side *x : {&s, &d})
+    if (x->img.rows <= 1) x->img.stride = x->img.row_bytes;
   s.on_device = device_accessible(src.ptr, &s.pinned);
   d.on_device = device_accessible(dst.ptr, &d.pinned);
   auto pitch_of = [](size_t row_bytes) { return (row_bytes + 255) / 256 * 256; };
