@@ -6,7 +6,7 @@ bool launch_fused_blurdown(const FilterJob &j, int *e, cudaStream_t s, cudaError
   return dispatch_channels<MODE_BLURDOWN, 5>(j, e, s, out, o, b);
 }
 size_t fused_smem_bytes(const FilterJob &job) {
-  return smem_layout(job.mode, job.ksize, job.threads, job.halo_chunks, job.box_lbw,
+  return smem_layout(job.mode, job.ksize, job.channels, job.threads, job.halo_chunks, job.box_lbw,
                      job.stage_rows, job.stages, job.use_tma != 0, job.border == BORDER_WRAP)
       .total;
 }

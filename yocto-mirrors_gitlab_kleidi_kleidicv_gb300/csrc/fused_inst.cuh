@@ -42,7 +42,7 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
         batch->jobs, batch->tiles, batch->ntiles, batch->next_tile, err_flag);
     return cudaGetLastError();
   }
-  const SmemLayout L = smem_layout(MODE, K, job.threads, job.halo_chunks, job.box_lbw,
+  const SmemLayout L = smem_layout(MODE, K, C, job.threads, job.halo_chunks, job.box_lbw,
                                    job.stage_rows, job.stages, job.use_tma != 0,
                                    job.border == BORDER_WRAP);
   auto kern = sepfused_kernel<MODE, K, C, NARROW>;

@@ -328,23 +328,25 @@ __device__ __forceinline__ uint32_t pair_at(const uint32_t (&lo)[NW], const uint
 // The words of a lane array that the lane-form horizontal pass reads,
 // relative to the lane's own first word: [first(), last()] (pair_at's word
 // w - HW, plus w + 1 - HW for pairs straddling two words).
+__host__ __device__ constexpr int lane_span_first(int k, int c) {
+  int m = 0;
+  for (int d = -(k / 2); d <= k / 2; ++d)
+    for (int p = 0; p < 2; ++p) m = floor_div(p + d * c, 4) < m ? floor_div(p + d * c, 4) : m;
+  return m;
+}
+__host__ __device__ constexpr int lane_span_last(int k, int c) {
+  int m = 3;
+  for (int d = -(k / 2); d <= k / 2; ++d)
+    for (int p = 0; p < 2; ++p) {
+      const int g = p + d * c, q = floor_div(g, 4), w = 3 + q + (g - 4 * q >= 2 ? 1 : 0);
+      m = w > m ? w : m;
+    }
+  return m;
+}
 template <int K, int C>
 struct LaneSpan {
-  static constexpr int first() {
-    int m = 0;
-    for (int d = -(K / 2); d <= K / 2; ++d)
-      for (int p = 0; p < 2; ++p) m = floor_div(p + d * C, 4) < m ? floor_div(p + d * C, 4) : m;
-    return m;
-  }
-  static constexpr int last() {
-    int m = 3;
-    for (int d = -(K / 2); d <= K / 2; ++d)
-      for (int p = 0; p < 2; ++p) {
-        const int g = p + d * C, q = floor_div(g, 4), w = 3 + q + (g - 4 * q >= 2 ? 1 : 0);
-        m = w > m ? w : m;
-      }
-    return m;
-  }
+  static constexpr int first() { return lane_span_first(K, C); }
+  static constexpr int last() { return lane_span_last(K, C); }
   // Words fetched from neighbouring lanes, per array.
   static constexpr int neighbour_words = (last() - 3) - first();
 };
@@ -355,11 +357,18 @@ struct LaneSpan {
 #ifndef KCV_SHUFFLE_WORDS
 #define KCV_SHUFFLE_WORDS 6
 #endif
+// Whether the horizontal pass of (mode, k, c) goes through the shared V rows
+// (host and device); Sobel and the shuffle modes need none.
+__host__ __device__ constexpr bool uses_v_rows(int mode, int k, int c) {
+  return mode == MODE_BLURDOWN ||
+         (mode != MODE_SOBEL_X && mode != MODE_SOBEL_Y &&
+          (mode == MODE_SEP_U16 || mode == MODE_SEP_S16
+               ? 2 * (k / 2) * c > KCV_SHUFFLE_WORDS  // one 32-bit word per element
+               : (lane_span_last(k, c) - 3) - lane_span_first(k, c) > KCV_SHUFFLE_WORDS));
+}
 template <int MODE, int K, int C>
 constexpr bool shuffle_horizontal() {
-  if constexpr (MODE == MODE_BLURDOWN || ModeTraits<MODE>::SOBEL) return false;
-  else if constexpr (ModeTraits<MODE>::LANES) return LaneSpan<K, C>::neighbour_words <= KCV_SHUFFLE_WORDS;
-  else return 2 * (K / 2) * C <= KCV_SHUFFLE_WORDS;  // u16/s16: one 32-bit word per element
+  return !ModeTraits<MODE>::SOBEL && !uses_v_rows(MODE, K, C);
 }
 
 // Fills the words of lo/hi that the horizontal pass reads from the lane's
@@ -683,9 +692,9 @@ struct SmemLayout {
   uint32_t ring_off, ring_rows, wrap_off, edge_off, edge_warp_bytes, v_off, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int mode, int k, int threads, int hc, int lbw,
-                                                  int stage_rows, int stages, bool use_tma,
-                                                  bool wrap) {
+__host__ __device__ inline SmemLayout smem_layout(int mode, int k, int c, int threads, int hc,
+                                                  int lbw, int stage_rows, int stages,
+                                                  bool use_tma, bool wrap) {
   const CtaShape s = cta_shape(threads, hc, lbw);
   SmemLayout l;
   l.ring_rows = static_cast<uint32_t>(stage_rows * stages);
@@ -697,7 +706,7 @@ __host__ __device__ inline SmemLayout smem_layout(int mode, int k, int threads, 
   l.edge_off = l.wrap_off + wrap_bytes;
   l.edge_warp_bytes = use_tma ? l.ring_rows * edge_slots(hc) * kChunk : 0;
   l.v_off = l.edge_off + s.warps * l.edge_warp_bytes;
-  l.total = l.v_off + s.warps * 2 * kVRowBytes;
+  l.total = l.v_off + (uses_v_rows(mode, k, c) ? s.warps * 2 * kVRowBytes : 0u);
   return l;
 }
 
@@ -730,7 +739,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   const int rb = j.stage_rows, ns = j.stages;
   const int lrb = __ffs(rb) - 1;
   const bool use_tma = j.use_tma != 0;
-  const SmemLayout L = smem_layout(MODE, K, blockDim.x, HC, lbw, rb, ns, use_tma,
+  const SmemLayout L = smem_layout(MODE, K, C, blockDim.x, HC, lbw, rb, ns, use_tma,
                                    j.border == BORDER_WRAP);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   uint64_t *empty = full + ns;
@@ -1152,6 +1161,9 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
 // ---------------------------------------------------------------------------
 // Launch: a grid of up to (resident CTAs per SM x SMs) CTAs that walk the
 // job's tiles (strip, band) in row-major band order; threads = 32 * warps.
+// Register budget: 4 resident CTAs per SM (2 for the 15/21 sizes).  Cutting
+// it for 5 (96 registers, which the shuffle modes fit without spilling) was
+// measured 7-11 % slower on 3840x2160 calls.
 template <int MODE, int K, int C, bool NARROW>
 __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
     sepfused_kernel(const __grid_constant__ FilterJob job, int *err_flag) {
