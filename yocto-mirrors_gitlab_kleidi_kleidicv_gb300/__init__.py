@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libkleidicv_gpu.so")
@@ -213,6 +214,10 @@ class Context:
             self.handle = None
 
     def __del__(self):
+        # At interpreter exit the CUDA runtime may already be gone: leave the
+        # release to process teardown instead of calling into it.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -389,6 +394,10 @@ class LKPyramid:
             self.handle = None
 
     def __del__(self):
+        # At interpreter exit the CUDA runtime may already be gone: leave the
+        # release to process teardown instead of calling into it.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -440,6 +449,10 @@ class BatchPlan:
             self.handle = None
 
     def __del__(self):
+        # At interpreter exit the CUDA runtime may already be gone: leave the
+        # release to process teardown instead of calling into it.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -498,6 +511,10 @@ class Server:
             self.handle = None
 
     def __del__(self):
+        # At interpreter exit the CUDA runtime may already be gone: leave the
+        # release to process teardown instead of calling into it.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

@@ -25,7 +25,10 @@ namespace kcv {
 namespace {
 
 constexpr int kBatchThreads = 128;  // every batched kernel runs 4-warp CTAs
-constexpr int kBatchTileRows = 32;  // output rows per tile (whole blocks)
+#ifndef KCV_BATCH_TILE_ROWS
+#define KCV_BATCH_TILE_ROWS 64
+#endif
+constexpr int kBatchTileRows = KCV_BATCH_TILE_ROWS;  // output rows per tile (whole blocks)
 constexpr int kMaxBranches = 8;
 
 struct Group {
@@ -188,7 +191,7 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
       }
       case Prepared::FUSED: {
         FilterJob j = pr.fused;
-        // The batched kernels run fixed 4-warp CTAs over 32-row tiles with the
+        // The batched kernels run fixed 4-warp CTAs over 64-row tiles with the
         // default ring (the autotune table is measured for whole-image calls).
         TileShape t{kBatchThreads, 0, 4, 0};
         // Whole blocks of output rows; bands are counted in 16 bits.
