@@ -72,7 +72,7 @@ def test_bounded_wait_timeout_is_reported_and_context_survives():
 
 
 SHAPES = [(64, 0, 2, 0), (96, 0, 8, 0), (128, 0, 2, 8), (128, 12, 4, 6), (96, 20, 4, 0), (32, 0, 4, 0),
-          (64, 0, 4, 8), (128, 0, 2, 6), (96, 0, 2, 0), (64, 0, 2, 8)]
+          (64, 0, 4, 8), (128, 0, 2, 6), (96, 0, 2, 0), (64, 0, 2, 8), (128, 0, 8, 0), (64, 0, 8, 6)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
