@@ -32,6 +32,14 @@ bool image_size_ok(size_t w, size_t h) {
   return n <= kMaxImagePixels;
 }
 
+// The kernels index rows and columns in 32-bit arithmetic: a row of more than
+// 2^30 bytes or more than 2^30 rows (images the reference accepts up to 2^48
+// pixels, but no GPU holds as one row) is refused with RANGE instead of being
+// processed wrongly.
+bool device_dims_ok(size_t row_bytes, size_t height) {
+  return row_bytes <= (size_t{1} << 30) && height <= (size_t{1} << 30);
+}
+
 // check_pointer_and_stride for 2-byte types (utils.h:379-390).
 bool stride_misaligned(size_t stride, size_t height, size_t elem) {
   return height > 1 && (stride % elem) != 0;
@@ -117,6 +125,7 @@ kleidicv_error_t prepare_gaussian(const uint8_t *src, size_t src_stride, uint8_t
     return KLEIDICV_ERROR_NOT_IMPLEMENTED;
   if (!src || !dst) return KLEIDICV_ERROR_NULL_POINTER;
   if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
+  if (!device_dims_ok(width * channels, height)) return KLEIDICV_ERROR_RANGE;
 
   *out = Prepared{};
   if (channels == 0) return KLEIDICV_OK;
@@ -199,6 +208,7 @@ kleidicv_error_t prepare_separable(int elem, const void *src, size_t src_stride,
   if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
   if (!kernel_x || !kernel_y) return KLEIDICV_ERROR_NULL_POINTER;
   if (channels > kMaxChannels) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!device_dims_ok(width * channels * es, height)) return KLEIDICV_ERROR_RANGE;
 
   *out = Prepared{};
   if (channels == 0) return KLEIDICV_OK;
@@ -247,6 +257,7 @@ kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t 
   if (!border_supported(border, ext)) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
   if (!src || !dst) return KLEIDICV_ERROR_NULL_POINTER;
   if (!image_size_ok(src_width, src_height)) return KLEIDICV_ERROR_RANGE;
+  if (!device_dims_ok(src_width * channels, src_height)) return KLEIDICV_ERROR_RANGE;
 
   *out = Prepared{};
   out->kind = Prepared::FUSED;
@@ -273,6 +284,7 @@ kleidicv_error_t prepare_sobel(bool horizontal, const uint8_t *src, size_t src_s
   if (stride_misaligned(dst_stride, height, 2)) return KLEIDICV_ERROR_ALIGNMENT;
   if (!image_size_ok(width, height)) return KLEIDICV_ERROR_RANGE;
   if (channels > kMaxChannels) return KLEIDICV_ERROR_NOT_IMPLEMENTED;
+  if (!device_dims_ok(2 * width * channels, height)) return KLEIDICV_ERROR_RANGE;
 
   *out = Prepared{};
   if (channels == 0) return KLEIDICV_OK;

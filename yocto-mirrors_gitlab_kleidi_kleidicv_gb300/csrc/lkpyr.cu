@@ -120,6 +120,10 @@ kleidicv_error_t kleidicv_gpu_build_optical_flow_pyr_lk_pyramid(
     lw = nw;
     lh = nh;
   }
+  // 32-bit row and column indexing on the device (bordered level 0, Scharr rows).
+  if ((width + 2 * window_width) * channels * 4 > (size_t{1} << 30) ||
+      height + 2 * window_height > (size_t{1} << 30))
+    return KLEIDICV_ERROR_RANGE;
   kleidicv_error_t e = resolve_context(ctx);
   if (e != KLEIDICV_OK) return e;
   DeviceGuard guard(ctx->device);

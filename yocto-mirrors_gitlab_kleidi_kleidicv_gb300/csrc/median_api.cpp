@@ -37,6 +37,9 @@ kleidicv_error_t median_blur(MedianElem elem, size_t es, const void *src, size_t
         height >= kernel_height - 1 && width >= kernel_width - 1 && kernel_ok && border_ok))
     return KLEIDICV_ERROR_NOT_IMPLEMENTED;
   if (channels == 0 || width == 0 || height == 0) return KLEIDICV_OK;
+  // 32-bit row and column indexing on the device (see the fused filters).
+  if (width * channels * es > (size_t{1} << 30) || height > (size_t{1} << 30))
+    return KLEIDICV_ERROR_RANGE;
 
   kleidicv_error_t e = kcv::resolve_context(ctx);
   if (e != KLEIDICV_OK) return e;
