@@ -213,3 +213,21 @@ def test_no_cpu_fallback(lib, kcv, no_gpu):
     got = lib.kleidicv_gpu_gaussian_blur_u8_noalloc(a.ctypes.data, 64, b.ctypes.data, 64, 64, 64, 1, 31, 31, 0.0,
                                                     0.0, 1, None)
     assert got == kcv.ERROR_NO_DEVICE
+
+
+def test_rows_beyond_32_bit_device_indexing_are_refused(lib, kcv):
+    """Valid for the reference (< 2^48 pixels) but rows over 2^30 bytes or more
+    than 2^30 rows: RANGE before any device work (no pointer is dereferenced)."""
+    big, tall = (1 << 30) + 16, (1 << 30) + 1
+    taps8 = (ctypes.c_uint8 * 5)(1, 1, 1, 1, 1)
+    taps16 = (ctypes.c_uint16 * 5)(1, 1, 1, 1, 1)
+    assert lib.kleidicv_gpu_gaussian_blur_u8(FAKE, big, FAKE, big, big, 8, 1, 5, 5, 0.0, 0.0, 1, None) == kcv.RANGE
+    assert lib.kleidicv_gpu_gaussian_blur_u8(FAKE, 64, FAKE, 64, 64, tall, 1, 5, 5, 0.0, 0.0, 1, None) == kcv.RANGE
+    assert lib.kleidicv_gpu_separable_filter_2d_u8(FAKE, big, FAKE, big, big, 8, 1, taps8, 5, taps8, 5, 2,
+                                                   None) == kcv.RANGE
+    assert lib.kleidicv_gpu_separable_filter_2d_u16(FAKE, 2 * big, FAKE, 2 * big, big // 2 + 8, 8, 1, taps16, 5,
+                                                    taps16, 5, 2, None) == kcv.RANGE
+    assert lib.kleidicv_gpu_blur_and_downsample_u8(FAKE, big, big, 8, FAKE, big, 1, 2, None) == kcv.RANGE
+    assert lib.kleidicv_gpu_sobel_3x3_horizontal_s16_u8(FAKE, big, FAKE, 2 * big, big // 2 + 8, 8, 1,
+                                                        None) == kcv.RANGE
+    assert lib.kleidicv_gpu_median_blur_u8(FAKE, big, FAKE + 16, big, big, 8, 1, 3, 3, 1, None) == kcv.RANGE
