@@ -63,7 +63,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="c1,batched,pyramid,sobel,median,thread_api,serving",
+    ap.add_argument("--sections", default="c1,batched,pyramid,lk_pyramid,sobel,median,thread_api,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
     ap.add_argument("--serving-seconds", type=float, default=3.0)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
@@ -624,6 +624,45 @@ def section_median(torch, kcv, ctx, stream):
     return out
 
 
+def section_lk_pyramid(torch, kcv, ctx, stream):
+    """kleidicv_gpu_build_optical_flow_pyr_lk_pyramid on 1920x1080x1, 4 levels,
+    21x21 window (seed 7): device time per build + release (bordered images
+    and Scharr pairs of every level, device memory from the context pool),
+    and level 1 (image and Scharr interiors) against the oracle."""
+    from oracle import oracle
+
+    w, h, c, levels, win = 1920, 1080, 1, 4, 21
+    rng = np.random.default_rng(7)
+    host = _pyr_image(rng, w, h, c)
+    src = torch.from_numpy(host).cuda()
+
+    def build(i):
+        pyr = kcv.LKPyramid(src.data_ptr(), w * c, w, h, c, levels, win, win, ctx)
+        assert pyr.error == kcv.OK, pyr.error
+        pyr.close()
+
+    for i in range(3):
+        build(i)
+    ms = _events_time(torch, stream, build, 20)
+    pyr = kcv.LKPyramid(src.data_ptr(), w * c, w, h, c, levels, win, win, ctx)
+    torch.cuda.synchronize()
+    lw, lh, img, istr, sch, sstr, bw, bh = pyr.level(1)
+    got_img = torch.empty(lh * istr, dtype=torch.uint8, device="cuda")
+    _copy_device(got_img.data_ptr(), img, (lh - 1) * istr + lw * c)
+    got_sch = torch.empty(lh * sstr, dtype=torch.uint8, device="cuda")
+    _copy_device(got_sch.data_ptr(), sch, (lh - 1) * sstr + lw * c * 4)
+    gi = got_img.cpu().numpy().reshape(lh, istr)[:, : lw * c]
+    gs = got_sch.cpu().numpy().reshape(lh, sstr)[:, : lw * c * 4].copy().view(np.int16)
+    pyr.close()
+    _, want = oracle.lk_pyramid(host, w, h, c, levels, win, win)
+    lv = want[1]
+    exact = bool(np.array_equal(gi, lv["image"][bh:bh + lh, bw * c:(bw + lw) * c]) and
+                 np.array_equal(gs, lv["scharr"]))
+    return {"config": "1920x1080x1, 4 levels, 21x21 window, seed 7; CUDA events over 20 build+release cycles",
+            "ms_per_build": round(ms, 4), "mpix_s_level0": round(w * h / (ms * 1e-3) / 1e6, 1),
+            "level1_bit_exact": exact}
+
+
 def _log_uniform(rng, lo, hi):
     return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
 
@@ -945,6 +984,8 @@ def run_sections(args, names):
                 out[name] = section_batched(torch, kcv, ctx, stream, cores)
             elif name == "pyramid":
                 out[name] = section_pyramid(torch, kcv, ctx, stream)
+            elif name == "lk_pyramid":
+                out[name] = section_lk_pyramid(torch, kcv, ctx, stream)
             elif name == "median":
                 out[name] = section_median(torch, kcv, ctx, stream)
             elif name == "thread_api":
