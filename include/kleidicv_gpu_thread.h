@@ -15,6 +15,8 @@
  *   kleidicv_gpu_thread_blur_and_downsample_u8    kleidicv_thread.h:482-485
  *   kleidicv_gpu_thread_sobel_3x3_{horizontal,vertical}_s16_u8
  *                                                 kleidicv_thread.h:489-492, 528-531
+ *   kleidicv_gpu_thread_median_blur_{s8,u8,u16,s16,u32,s32,f32}
+ *                                                 kleidicv_thread.h:496-524
  *
  * The scheduler's tasks are row stripes of the host copies: in the upload
  * phase a task packs its source rows into pinned staging memory and enqueues
@@ -86,6 +88,37 @@ kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8(
 kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8(
     const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
     size_t height, size_t channels, kleidicv_thread_multithreading mt);
+
+/* kleidicv_thread_median_blur_* (kleidicv_thread.h:496-524, u32/s32 from the
+ * thread API's other element types). */
+kleidicv_error_t kleidicv_gpu_thread_median_blur_s8(
+    const int8_t *src, size_t src_stride, int8_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_u8(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_u16(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_s16(
+    const int16_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_u32(
+    const uint32_t *src, size_t src_stride, uint32_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_s32(
+    const int32_t *src, size_t src_stride, int32_t *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
+kleidicv_error_t kleidicv_gpu_thread_median_blur_f32(
+    const float *src, size_t src_stride, float *dst, size_t dst_stride, size_t width, size_t height,
+    size_t channels, size_t kernel_width, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
 
 /* A persistent worker pool implementing kleidicv_thread_parallel: `threads`
  * workers (0: the hardware concurrency) plus the calling thread take task

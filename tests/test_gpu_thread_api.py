@@ -115,3 +115,21 @@ def test_failing_scheduler_fails_the_call():
     assert LIB.kleidicv_gpu_thread_gaussian_blur_u8(host.ctypes.data, 300, dst.ctypes.data, 300, 300, 200, 1, 5, 5,
                                                     0.0, 0.0, kcv.REFLECT, POOL.mt) == kcv.OK
     assert np.array_equal(dst, oracle.gaussian_blur_u8(host, 300, 200, 1, 5, 0.0, kcv.REFLECT)[1])
+
+
+@pytest.mark.parametrize("combo", COMBOS, ids=lambda c: f"{c[0]}-{c[1]}")
+@pytest.mark.parametrize("dtype,k", [("u8", 5), ("f32", 3), ("s16", 7), ("u8", 15)])
+def test_median_threaded(combo, dtype, k):
+    rng = np.random.default_rng(k)
+    w, h, c = 301, 97, 2
+    dt = oracle.MEDIAN_DTYPES[dtype]
+    if np.dtype(dt).kind == "f":
+        host = rng.uniform(-100, 100, (h, w * c)).astype(dt)
+    else:
+        info = np.iinfo(dt)
+        host = rng.integers(info.min, int(info.max) + 1, (h, w * c), dtype=dt)
+    src, dst = Img(host, combo[0]), Img(np.zeros_like(host), combo[1])
+    fn = getattr(LIB, f"kleidicv_gpu_thread_median_blur_{dtype}")
+    stride = w * c * host.itemsize
+    assert fn(src.ptr, stride, dst.ptr, stride, w, h, c, k, k, kcv.REFLECT, POOL.mt) == kcv.OK
+    assert np.array_equal(dst.read(), oracle.median_blur(host, w, h, c, k, kcv.REFLECT))

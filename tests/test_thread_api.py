@@ -114,3 +114,31 @@ def test_entries_validate_then_need_a_scheduler(lib, kcv, oracle, no_gpu):
             assert not b.any()
     finally:
         pool.close()
+
+
+@pytest.mark.parametrize("dtype", ["s8", "u8", "u16", "s16", "u32", "s32", "f32"])
+def test_threaded_median_validates_like_the_reference(lib, kcv, oracle, no_gpu, dtype):
+    pool = kcv.ThreadPool(2)
+    fn = getattr(lib, f"kleidicv_gpu_thread_median_blur_{dtype}")
+    es = {"s8": 1, "u8": 1, "u16": 2, "s16": 2, "u32": 4, "s32": 4, "f32": 4}[dtype]
+    a = np.zeros(4096, np.uint8)
+    b = np.zeros(4096, np.uint8)
+    try:
+        for (w, h, c, k, border, sstride) in [(10, 10, 1, 5, 1, 64), (10, 10, 5, 5, 1, 64), (10, 10, 1, 4, 1, 64),
+                                              (10, 10, 1, 9, 1, 64), (10, 10, 1, 5, 0, 64), (3, 10, 1, 7, 1, 64),
+                                              (10, 10, 1, 5, 1, 63), (10, 10, 0, 5, 1, 64)]:
+            want = oracle.median_blur_check(dtype, False, sstride, False, 64, w, h, c, k, k, border)
+            got = fn(a.ctypes.data, sstride, b.ctypes.data, 64, w, h, c, k, k, border, pool.mt)
+            if want != 0:
+                assert got == want, (w, h, c, k, border, sstride, got, want)
+            elif c == 0:
+                assert got == kcv.OK
+            elif no_gpu:
+                assert got == kcv.ERROR_NO_DEVICE and not b.any()
+        assert fn(None, 64, b.ctypes.data, 64, 10, 10, 1, 5, 5, 1, pool.mt) == kcv.NULL_POINTER
+        assert fn(a.ctypes.data, 64, b.ctypes.data, 64, 10, 10, 1, 5, 5, 1, kcv.ThreadMT(None, None)) == \
+            kcv.NULL_POINTER
+        if es > 1:  # median validation checks the source stride's alignment first
+            assert fn(a.ctypes.data, 64 + 1, b.ctypes.data, 64, 10, 10, 1, 5, 5, 1, pool.mt) == kcv.ALIGNMENT
+    finally:
+        pool.close()

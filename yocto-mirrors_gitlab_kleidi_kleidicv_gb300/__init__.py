@@ -99,6 +99,8 @@ SIGNATURES = {
     "kleidicv_gpu_thread_blur_and_downsample_u8": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, ThreadMT]),
     "kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, ThreadMT]),
     "kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, ThreadMT]),
+    **{f"kleidicv_gpu_thread_median_blur_{t}": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _i, ThreadMT])
+       for t in ("s8", "u8", "u16", "s16", "u32", "s32", "f32")},
     "kleidicv_gpu_thread_pool_create": (_i, [ctypes.POINTER(_vp), ctypes.c_uint]),
     "kleidicv_gpu_thread_pool_destroy": (_i, [_vp]),
     "kleidicv_gpu_thread_pool_parallel": (_i, [_vp, _vp, _vp, ctypes.c_uint]),

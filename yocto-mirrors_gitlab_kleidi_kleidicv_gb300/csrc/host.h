@@ -79,6 +79,13 @@ kleidicv_error_t prepare_blurdown(const uint8_t *src, size_t src_stride, size_t 
                                   size_t channels, int border, bool ext, int border_value,
                                   Prepared *out);
 
+// Median blur checks in the reference's order (median_blur.h:148-193); *work is
+// false when a valid call has nothing to compute.  elem: a MedianElem.
+kleidicv_error_t validate_median(int elem, size_t es, const void *src, size_t src_stride,
+                                 const void *dst, size_t dst_stride, size_t width, size_t height,
+                                 size_t channels, size_t kernel_width, size_t kernel_height,
+                                 int border, bool *work);
+
 // horizontal: the x derivative (sobel_3x3_horizontal), else the y derivative.
 kleidicv_error_t prepare_sobel(bool horizontal, const uint8_t *src, size_t src_stride,
                                int16_t *dst, size_t dst_stride, size_t width, size_t height,

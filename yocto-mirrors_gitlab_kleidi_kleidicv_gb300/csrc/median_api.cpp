@@ -7,16 +7,15 @@
 
 #include "host.h"
 
-namespace {
-
-using kcv::MedianElem;
+namespace kcv {
 
 constexpr uint64_t kMaxImagePixels = (1ull << 48) - 1;  // kleidicv.h:103
 
-kleidicv_error_t median_blur(MedianElem elem, size_t es, const void *src, size_t src_stride,
-                             void *dst, size_t dst_stride, size_t width, size_t height,
-                             size_t channels, size_t kernel_width, size_t kernel_height,
-                             kleidicv_border_type_t border, kleidicv_gpu_context_t *ctx) {
+kleidicv_error_t validate_median(int elem, size_t es, const void *src, size_t src_stride,
+                                 const void *dst, size_t dst_stride, size_t width, size_t height,
+                                 size_t channels, size_t kernel_width, size_t kernel_height,
+                                 int border, bool *work) {
+  *work = false;
   // check_ptrs_strides_imagesizes (median_blur.h:148-158).
   if (!src) return KLEIDICV_ERROR_NULL_POINTER;
   if (height > 1 && src_stride % es != 0) return KLEIDICV_ERROR_ALIGNMENT;
@@ -26,7 +25,7 @@ kleidicv_error_t median_blur(MedianElem elem, size_t es, const void *src, size_t
   if (__builtin_mul_overflow(width, height, &pixels) || pixels > kMaxImagePixels)
     return KLEIDICV_ERROR_RANGE;
   // is_kernel_size_supported (:160-171) and the rest of :173-193.
-  const size_t kmax = elem == kcv::MEDIAN_U8 ? 255 : 7;
+  const size_t kmax = elem == MEDIAN_U8 ? 255 : 7;
   const bool kernel_ok = kernel_width == kernel_height && kernel_width >= 3 &&
                          kernel_width <= kmax && (kernel_width % 2) != 0;
   const bool border_ok = border == KLEIDICV_BORDER_TYPE_REPLICATE ||
@@ -40,6 +39,25 @@ kleidicv_error_t median_blur(MedianElem elem, size_t es, const void *src, size_t
   // 32-bit row and column indexing on the device (see the fused filters).
   if (width * channels * es > (size_t{1} << 30) || height > (size_t{1} << 30))
     return KLEIDICV_ERROR_RANGE;
+  *work = true;
+  return KLEIDICV_OK;
+}
+
+}  // namespace kcv
+
+namespace {
+
+using kcv::MedianElem;
+
+kleidicv_error_t median_blur(MedianElem elem, size_t es, const void *src, size_t src_stride,
+                             void *dst, size_t dst_stride, size_t width, size_t height,
+                             size_t channels, size_t kernel_width, size_t kernel_height,
+                             kleidicv_border_type_t border, kleidicv_gpu_context_t *ctx) {
+  bool work = false;
+  const kleidicv_error_t v =
+      kcv::validate_median(elem, es, src, src_stride, dst, dst_stride, width, height, channels,
+                           kernel_width, kernel_height, border, &work);
+  if (v != KLEIDICV_OK || !work) return v;
 
   kleidicv_error_t e = kcv::resolve_context(ctx);
   if (e != KLEIDICV_OK) return e;

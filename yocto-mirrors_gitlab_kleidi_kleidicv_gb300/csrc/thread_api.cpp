@@ -419,6 +419,55 @@ static kleidicv_error_t thread_sobel(bool horizontal, const uint8_t *src, size_t
       mt);
 }
 
+}  // extern "C"
+
+template <typename T>
+static kleidicv_error_t thread_median(kcv::MedianElem elem, const T *src, size_t src_stride, T *dst,
+                                      size_t dst_stride, size_t width, size_t height,
+                                      size_t channels, size_t kernel_width, size_t kernel_height,
+                                      kleidicv_border_type_t border_type,
+                                      kleidicv_thread_multithreading mt,
+                                      kleidicv_error_t (*entry)(const T *, size_t, T *, size_t, size_t,
+                                                                size_t, size_t, size_t, size_t,
+                                                                kleidicv_border_type_t,
+                                                                kleidicv_gpu_context_t *)) {
+  bool work = false;
+  const kleidicv_error_t v =
+      kcv::validate_median(elem, sizeof(T), src, src_stride, dst, dst_stride, width, height,
+                           channels, kernel_width, kernel_height, border_type, &work);
+  Prepared p;  // NOTHING unless the call has work
+  if (work) p.kind = Prepared::FUSED;
+  const size_t rb = width * channels * sizeof(T);
+  return run_threaded(
+      v, p, {reinterpret_cast<const uint8_t *>(src), src_stride, rb, height},
+      {reinterpret_cast<const uint8_t *>(dst), dst_stride, rb, height},
+      [&](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return entry(static_cast<const T *>(s), ss, static_cast<T *>(d), ds, width, height, channels,
+                     kernel_width, kernel_height, border_type, c);
+      },
+      mt);
+}
+
+extern "C" {
+
+#define KCV_THREAD_MEDIAN(suffix, T, ELEM)                                                     \
+  kleidicv_error_t kleidicv_gpu_thread_median_blur_##suffix(                                   \
+      const T *src, size_t src_stride, T *dst, size_t dst_stride, size_t width, size_t height, \
+      size_t channels, size_t kernel_width, size_t kernel_height,                              \
+      kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt) {                 \
+    return thread_median<T>(kcv::ELEM, src, src_stride, dst, dst_stride, width, height,        \
+                            channels, kernel_width, kernel_height, border_type, mt,            \
+                            kleidicv_gpu_median_blur_##suffix);                                \
+  }
+KCV_THREAD_MEDIAN(s8, int8_t, MEDIAN_S8)
+KCV_THREAD_MEDIAN(u8, uint8_t, MEDIAN_U8)
+KCV_THREAD_MEDIAN(u16, uint16_t, MEDIAN_U16)
+KCV_THREAD_MEDIAN(s16, int16_t, MEDIAN_S16)
+KCV_THREAD_MEDIAN(u32, uint32_t, MEDIAN_U32)
+KCV_THREAD_MEDIAN(s32, int32_t, MEDIAN_S32)
+KCV_THREAD_MEDIAN(f32, float, MEDIAN_F32)
+#undef KCV_THREAD_MEDIAN
+
 kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_horizontal_s16_u8(
     const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride, size_t width,
     size_t height, size_t channels, kleidicv_thread_multithreading mt) {
