@@ -17,10 +17,12 @@
 //     source rows of its chunk from the ring once, unpacks each once (u8 as
 //     packed 16-bit lanes) and adds it into the M vertical sums it belongs
 //     to, in the reference's intermediate width and rounding;
-//   * the M vertical rows go to the warp's shared V rows, then the
-//     horizontal pass reads its neighbours' lanes at compile-time offsets
-//     (tap distance = channels elements) one output row at a time, and the
-//     result is stored with 16-byte stores.
+//   * the horizontal pass then takes one output row at a time and reads the
+//     neighbouring lanes' vertical results at compile-time offsets (tap
+//     distance = channels elements): by warp shuffle straight from their
+//     registers when the halo is at most six words per lane array, otherwise
+//     through the warp's two shared V rows; the result is stored with
+//     16-byte stores (32-byte for the Sobel derivatives).
 //
 // Every output byte equals the reference's: the arithmetic per mode follows
 // kleidicv/src/filters/gaussian_blur_fixed_neon.cpp (binomial 3/5/7/9 and
