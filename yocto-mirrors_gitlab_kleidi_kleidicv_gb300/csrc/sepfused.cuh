@@ -1066,10 +1066,11 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
                                     static_cast<uint32_t>(ring_rows), tp, v);
     rq += MODE == MODE_BLURDOWN ? 2 * M : M;
     if (rq >= ring_rows) rq -= ring_rows;
-    // ---- horizontal pass + store, one output row at a time through the
-    // warp's two V rows: write row m, __syncwarp, read it.  Row m + 2 reuses
-    // the buffer only after the __syncwarp of row m + 1, when every lane has
-    // finished reading row m.
+    // ---- horizontal pass + store, one output row at a time.  Shuffle modes
+    // (and Sobel) take the neighbours' words from registers.  The others go
+    // through the warp's two V rows: write row m, __syncwarp, read it; row
+    // m + 2 reuses the buffer only after the __syncwarp of row m + 1, when
+    // every lane has finished reading row m.
     const int mcount = min(M, orows - ob);
     // This lane's destination chunk in the block's first row.
     uint8_t *const dblock =
