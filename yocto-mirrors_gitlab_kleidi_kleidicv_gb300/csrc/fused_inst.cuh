@@ -9,6 +9,24 @@
 
 namespace kcv {
 
+// Raises kernel Kern's dynamic shared-memory limit once per device (the
+// attribute is per device); safe under concurrent first calls.  The kernel is
+// a template argument so that every kernel has its own flags.
+template <auto Kern>
+cudaError_t allow_large_smem() {
+  constexpr int kMaxDevices = 64;
+  static std::once_flag once[kMaxDevices];
+  static cudaError_t err[kMaxDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::call_once(once[dev], [&] {
+    err[dev] = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  });
+  return err[dev];
+}
+
 // Plain launch of `job` (batch == nullptr) or of the batched kernel of the
 // same instantiation over batch->tiles.  With blocks_per_sm set, only reports
 // the occupancy.
@@ -17,13 +35,7 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
                        int *blocks_per_sm, const BatchLaunch *batch) {
   if (batch) {
     auto kern = batch_kernel<MODE, K, C, NARROW>;
-    static bool battr_set = false;  // per instantiation
-    if (!battr_set) {
-      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           200 * 1024);
-      if (e != cudaSuccess) return e;
-      battr_set = true;
-    }
+    if (cudaError_t e = allow_large_smem<batch_kernel<MODE, K, C, NARROW>>(); e != cudaSuccess) return e;
     if (blocks_per_sm) {
       // Cached per instantiation for the last shared-memory size asked.
       static size_t cached_smem = ~static_cast<size_t>(0);
@@ -46,13 +58,8 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
                                    job.stage_rows, job.stages, job.use_tma != 0,
                                    job.border == BORDER_WRAP);
   auto kern = sepfused_kernel<MODE, K, C, NARROW>;
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  if (cudaError_t e = allow_large_smem<sepfused_kernel<MODE, K, C, NARROW>>(); e != cudaSuccess)
+    return e;
   // One wave of persistent CTAs: as many as fit on the device at once.
   int per_sm = 0, dev = 0, sms = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, job.threads, L.total);
