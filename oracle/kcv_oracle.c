@@ -195,6 +195,29 @@ static int arbitrary_h_saturates(const ko_job *j, long x) {
   return wc - 2 * bl >= 16;
 }
 
+/* Arbitrary-size right border (gaussian_blur_arbitrary_neon.cpp:346-377,
+ * border_generic_neon.h:80-98).  The last `arb_border_len` elements of a row
+ * are computed by 8-lane vectors starting at width*channels - arb_border_len.
+ * For the right-hand tap at distance d (columns) the vector starting at xv
+ * reads elements xv + c*d .. +7; when all of them lie past the row end, the
+ * reference builds the replicated lanes from an index pattern that, for
+ * q = (xv + c*d - width*c) % c != 0, gives lanes 8-q..7 channel lane+c-8 of
+ * the last pixel instead of channel (q+lane) % c.  Returns that channel for
+ * output element e and tap distance d, or -1 where the lane is exact. */
+static long arb_right_lane_channel(const ko_job *j, long e, long d) {
+  const long c = (long)j->channels;
+  const long wc = (long)j->width * c;
+  const long bl = (long)j->arb_border_len;
+  if (c == 1 || e < wc - bl) return -1;
+  const long xv = wc - bl + (e - (wc - bl)) / 8 * 8;
+  const long lane = e - xv;
+  const long start = xv + c * d;
+  if (start < wc) return -1;
+  const long q = (start - wc) % c;
+  if (q == 0 || lane < 8 - q) return -1;
+  return lane + c - 8;
+}
+
 /* Horizontal pass for one output element given the K intermediate values. */
 static int64_t horizontal(const ko_job *j, const int64_t *v, long x) {
   const int k = j->ksize;
@@ -253,6 +276,12 @@ static void run_rows(const ko_job *j, size_t y0, size_t y1, int64_t *vrow) {
         for (long t = 0; t < j->ksize; ++t) {
           const long rc = ko_border_map(col + t - r, w, j->border);
           v[t] = rc < 0 ? v_const : vrow[rc * c + ch];
+        }
+        if (j->arbitrary) {
+          for (long d = 1; d <= r; ++d) {
+            const long qc = arb_right_lane_channel(j, ox * c + ch, d);
+            if (qc >= 0) v[r + d] = vrow[(w - 1) * c + qc];
+          }
         }
         store_elem(j, (long)oy, ox * c + ch, horizontal(j, v, ox * c + ch));
       }

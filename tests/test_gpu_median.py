@@ -107,3 +107,13 @@ def test_rejections():
     assert kcv.median_blur("u8", p, 64, p + 8192, 64, 10, 10, 1, 5, 5, kcv.CONSTANT, ctx) == kcv.NOT_IMPLEMENTED
     assert ctx.synchronize() == kcv.OK
     ctx.close()
+
+
+@pytest.mark.parametrize("case", [(4, 270000, 1, 3), (9, 70000, 1, 9)])
+def test_tall_narrow_images(case):
+    """Heights beyond the grid's 65535-block y limit: the small-window kernel
+    (four rows per block) and the sliding-histogram kernel (one row per block)
+    both loop over rows."""
+    w, h, c, k = case
+    got, want, pad_ok = run("u8", w, h, c, k, 1, 21)
+    assert pad_ok and np.array_equal(got, want)

@@ -269,3 +269,20 @@ def test_config_4k_separable(kcv, oracle, ctx, dt, border):
     err, want = oracle.separable_filter_2d(host, 3840, 2160, 1, kx.astype(dtype), ky.astype(dtype), border,
                                            ext=bv is not None, border_value=bv or 0, nthreads=16)
     assert err == 0 and np.array_equal(got, want)
+
+
+def test_arbitrary_size_tall_narrow_image(kcv, oracle, ctx):
+    """A 13x70000 image with an 11x11 generated kernel: more rows than the
+    grid's 65535-block y limit in both passes of the two-pass kernel."""
+    rng = np.random.default_rng(70000)
+    check_gaussian(kcv, oracle, ctx, rng, 13, 70000, 1, 11, 2.0, 1)
+
+
+@pytest.mark.parametrize("c", [2, 3, 4])
+@pytest.mark.parametrize("k,w", [(11, 13), (13, 21), (17, 47), (31, 40), (63, 71), (101, 301)])
+def test_arbitrary_size_right_border_lanes(kcv, oracle, ctx, k, w, c):
+    """Arbitrary sizes with 2-4 channels: the right-border vectors' replicated
+    lanes take the reference's shifted channel pattern."""
+    rng = np.random.default_rng(k * 10 + c)
+    for sigma in (0.0, 3.0):
+        check_gaussian(kcv, oracle, ctx, rng, w, k + 3, c, k, sigma, 1)

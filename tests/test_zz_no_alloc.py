@@ -1,17 +1,23 @@
-"""kleidicv_gpu_gaussian_blur_u8_noalloc against kleidicv_gpu_gaussian_blur_u8.
+"""kleidicv_gpu_gaussian_blur_u8_noalloc against kleidicv_gpu_gaussian_blur_u8
+and the CPU oracle.
 
-The allocation-free entry must give the same bytes as the context entry for
-the requests it serves (two-pass arbitrary-size kernel, plain copy), on
-consecutive calls that reuse its one scratch buffer, and must reject what it
-does not serve.  This file is collected last so that it also runs after every
-other GPU test has used the device.
+The allocation-free entry must give the same bytes as the context entry (and
+as the oracle) for the requests it serves (two-pass arbitrary-size kernel,
+plain copy), on consecutive calls that reuse its one scratch buffer; repeated
+calls must leave the device's free memory and torch's allocator untouched;
+and it must reject what it does not serve.  This file is collected last so
+that it also runs after every other GPU test has used the device.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
 import __graft_entry__ as ge  # noqa: E402
+from oracle import oracle  # noqa: E402
+from tests.gpu_harness import _cudart  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +65,43 @@ def test_two_calls_in_a_row_match_context_entry():
         assert err == kcv.OK
         assert ctx.synchronize() == kcv.OK
         assert torch.equal(got, want), f"k={k}: {(got != want).sum().item()} bytes differ"
+        oerr, owant = oracle.gaussian_blur_u8(src.cpu().numpy(), w, h, c, k, s, kcv.REPLICATE, nthreads=8)
+        assert oerr == oracle.OK
+        assert np.array_equal(got.cpu().numpy()[:, : w * c], owant), f"k={k}: differs from the oracle"
     ctx.close()
+
+
+def _free_device_bytes():
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert _cudart().cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_repeated_calls_allocate_nothing():
+    """After one warm-up call (which resolves the scratch buffer's address),
+    further calls change neither the device's free memory nor torch's
+    allocator counters."""
+    rng = np.random.default_rng(14)
+    w, h, c, k = 1203, 777, 3, 23
+    src = _image(rng, w, h, c)
+    dst = torch.empty((h, w * c), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        return kcv.gaussian_blur_u8_noalloc(src.data_ptr(), src.stride(0), dst.data_ptr(), dst.stride(0),
+                                            w, h, c, k, k, 3.0, 3.0, kcv.REPLICATE, s)
+
+    assert call() == kcv.OK
+    torch.cuda.synchronize()
+    free0 = _free_device_bytes()
+    allocs0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    for _ in range(20):
+        assert call() == kcv.OK
+    torch.cuda.synchronize()
+    assert _free_device_bytes() == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == allocs0
+    oerr, want = oracle.gaussian_blur_u8(src.cpu().numpy(), w, h, c, k, 3.0, kcv.REPLICATE, nthreads=8)
+    assert oerr == oracle.OK and np.array_equal(dst.cpu().numpy(), want)
 
 
 def test_copy_kernel_matches():

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "launch.h"
@@ -9,22 +10,26 @@
 
 namespace kcv {
 
+constexpr int kMaxDevices = 64;
+
 // Raises kernel Kern's dynamic shared-memory limit once per device (the
-// attribute is per device); safe under concurrent first calls.  The kernel is
-// a template argument so that every kernel has its own flags.
+// attribute is per device); safe under concurrent first calls.  A failed
+// attempt is not remembered: the next launch on that device tries again.  The
+// kernel is a template argument so that every kernel has its own flags.
 template <auto Kern>
 cudaError_t allow_large_smem() {
-  constexpr int kMaxDevices = 64;
-  static std::once_flag once[kMaxDevices];
-  static cudaError_t err[kMaxDevices];
+  static std::atomic<bool> done[kMaxDevices];  // zero-initialised: false
+  static std::mutex m;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::call_once(once[dev], [&] {
-    err[dev] = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  });
-  return err[dev];
+  if (done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(m);
+  if (done[dev].load(std::memory_order_relaxed)) return cudaSuccess;
+  e = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess) done[dev].store(true, std::memory_order_release);
+  return e;
 }
 
 // Plain launch of `job` (batch == nullptr) or of the batched kernel of the
@@ -37,17 +42,22 @@ cudaError_t launch_one(const FilterJob &job, int *err_flag, cudaStream_t stream,
     auto kern = batch_kernel<MODE, K, C, NARROW>;
     if (cudaError_t e = allow_large_smem<batch_kernel<MODE, K, C, NARROW>>(); e != cudaSuccess) return e;
     if (blocks_per_sm) {
-      // Cached per instantiation for the last shared-memory size asked.
-      static size_t cached_smem = ~static_cast<size_t>(0);
-      static int cached_occ = 0;
+      // Cached per instantiation and device for the last shared-memory size asked.
+      static size_t cached_smem[kMaxDevices];
+      static int cached_occ[kMaxDevices];
+      static bool valid[kMaxDevices];
       static std::mutex m;
+      int dev = 0;
+      if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return e;
+      if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
       std::lock_guard<std::mutex> lock(m);
-      if (cached_smem != batch->smem) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_occ, kern, 128, batch->smem);
+      if (!valid[dev] || cached_smem[dev] != batch->smem) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_occ[dev], kern, 128, batch->smem);
         if (e != cudaSuccess) return e;
-        cached_smem = batch->smem;
+        cached_smem[dev] = batch->smem;
+        valid[dev] = true;
       }
-      *blocks_per_sm = cached_occ;
+      *blocks_per_sm = cached_occ[dev];
       return cudaSuccess;
     }
     kern<<<static_cast<unsigned>(batch->grid), 128, batch->smem, stream>>>(

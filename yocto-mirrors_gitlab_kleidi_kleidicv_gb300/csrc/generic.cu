@@ -42,33 +42,36 @@ __global__ void __launch_bounds__(256) generic_vertical(const __grid_constant__ 
   const long x = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
   if (x >= wc) return;
   const int ne = static_cast<int>(wc - x < 4 ? wc - x : 4);
-  const int y0 = blockIdx.y * kRowsPerThread;
-  const int y1 = min(y0 + kRowsPerThread, j.height);
   const int r = j.ksize / 2;
-  for (int y = y0; y < y1; ++y) {
-    uint32_t acc[4] = {0, 0, 0, 0};
-    for (int t = 0; t < j.ksize; ++t) {
-      const int ry = map_index(y + t - r, j.height, j.border);
-      const uint32_t g = weight(j, t);
-      if (ry < 0) {
-        const uint32_t bv = static_cast<uint32_t>(j.border_value) & 0xFFu;
-        for (int e = 0; e < 4; ++e) acc[e] += g * bv;
-      } else {
-        const uint8_t *row = j.src + static_cast<int64_t>(ry) * j.src_stride + x;
-        if (ne == 4 && (reinterpret_cast<uintptr_t>(row) & 3) == 0) {
-          const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(row));
-          acc[0] += g * (w & 0xFFu);
-          acc[1] += g * ((w >> 8) & 0xFFu);
-          acc[2] += g * ((w >> 16) & 0xFFu);
-          acc[3] += g * (w >> 24);
+  // Row blocks loop over the grid's y extent, which the hardware caps at 65535.
+  for (long yb = blockIdx.y; yb * kRowsPerThread < j.height; yb += gridDim.y) {
+    const int y0 = static_cast<int>(yb * kRowsPerThread);
+    const int y1 = min(y0 + kRowsPerThread, j.height);
+    for (int y = y0; y < y1; ++y) {
+      uint32_t acc[4] = {0, 0, 0, 0};
+      for (int t = 0; t < j.ksize; ++t) {
+        const int ry = map_index(y + t - r, j.height, j.border);
+        const uint32_t g = weight(j, t);
+        if (ry < 0) {
+          const uint32_t bv = static_cast<uint32_t>(j.border_value) & 0xFFu;
+          for (int e = 0; e < 4; ++e) acc[e] += g * bv;
         } else {
-          for (int e = 0; e < ne; ++e) acc[e] += g * __ldg(row + e);
+          const uint8_t *row = j.src + static_cast<int64_t>(ry) * j.src_stride + x;
+          if (ne == 4 && (reinterpret_cast<uintptr_t>(row) & 3) == 0) {
+            const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(row));
+            acc[0] += g * (w & 0xFFu);
+            acc[1] += g * ((w >> 8) & 0xFFu);
+            acc[2] += g * ((w >> 16) & 0xFFu);
+            acc[3] += g * (w >> 24);
+          } else {
+            for (int e = 0; e < ne; ++e) acc[e] += g * __ldg(row + e);
+          }
         }
       }
+      uint8_t *out = vbuf + static_cast<int64_t>(y) * vstride + x;
+      for (int e = 0; e < ne; ++e)
+        out[e] = static_cast<uint8_t>(j.vert_saturates ? round_sat(acc[e]) : round_wrap(acc[e]));
     }
-    uint8_t *out = vbuf + static_cast<int64_t>(y) * vstride + x;
-    for (int e = 0; e < ne; ++e)
-      out[e] = static_cast<uint8_t>(j.vert_saturates ? round_sat(acc[e]) : round_wrap(acc[e]));
   }
 }
 
@@ -79,6 +82,25 @@ __device__ __forceinline__ bool h_saturates(const GenericJob &j, long x, long wc
   return wc - 2 * bl >= 16;
 }
 
+// Right-border lane channel of the arbitrary-size path.  The reference
+// computes the last arb_border_len elements of a row with 8-lane vectors that
+// start at width*channels - arb_border_len; for the right-hand tap at distance
+// d columns, a vector starting at xv whose lanes xv + c*d .. +7 all lie past
+// the row end takes its replicated lanes from an index pattern that gives
+// lanes 8-q..7 channel lane+c-8 of the last pixel, q = (xv + c*d) % c, instead
+// of channel (q + lane) % c (border_generic_neon.h:80-98,
+// gaussian_blur_arbitrary_neon.cpp:346-377).  Returns that channel, or -1
+// where the lane is exact.
+__device__ __forceinline__ int right_lane_channel(long e, int d, int c, long wc, long bl) {
+  const long xv = wc - bl + (e - (wc - bl)) / 8 * 8;
+  const int lane = static_cast<int>(e - xv);
+  const long start = xv + static_cast<long>(c) * d;
+  if (start < wc) return -1;
+  const int q = static_cast<int>((start - wc) % c);
+  if (q == 0 || lane < 8 - q) return -1;
+  return lane + c - 8;
+}
+
 __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_constant__ GenericJob j,
                                                                 const uint8_t *vbuf,
                                                                 size_t vstride) {
@@ -86,34 +108,45 @@ __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_con
   const int c = j.channels;
   const int r = j.ksize / 2;
   const long wc = static_cast<long>(j.width) * c;
-  const int y = blockIdx.y;
   const long x0 = static_cast<long>(blockIdx.x) * kHElems;
   const int halo = r * c;
   const int seg_len = kHElems + 2 * halo;
-  const uint8_t *vrow = vbuf + static_cast<int64_t>(y) * vstride;
-  // Stage [x0 - halo, x0 + kHElems + halo) with the border resolved per element.
-  for (int i = threadIdx.x; i < seg_len; i += blockDim.x) {
-    const long xe = x0 - halo + i;
-    uint8_t v;
-    if (xe >= 0 && xe < wc) {
-      v = vrow[xe];
-    } else {
-      const long col = xe >= 0 ? xe / c : -((-xe + c - 1) / c);
-      const int ch = static_cast<int>(xe - col * c);
-      const int mc = map_index(static_cast<int>(col), j.width, j.border);
-      v = mc < 0 ? static_cast<uint8_t>(j.v_const) : vrow[static_cast<long>(mc) * c + ch];
+  const bool right_quirk = j.arbitrary && c > 1 && x0 + kHElems > wc - j.arb_border_len;
+  // Rows loop over the grid's y extent, which the hardware caps at 65535.
+  for (int y = blockIdx.y; y < j.height; y += gridDim.y) {
+    const uint8_t *vrow = vbuf + static_cast<int64_t>(y) * vstride;
+    __syncthreads();  // the previous row's reads of seg are done
+    // Stage [x0 - halo, x0 + kHElems + halo) with the border resolved per element.
+    for (int i = threadIdx.x; i < seg_len; i += blockDim.x) {
+      const long xe = x0 - halo + i;
+      uint8_t v;
+      if (xe >= 0 && xe < wc) {
+        v = vrow[xe];
+      } else {
+        const long col = xe >= 0 ? xe / c : -((-xe + c - 1) / c);
+        const int ch = static_cast<int>(xe - col * c);
+        const int mc = map_index(static_cast<int>(col), j.width, j.border);
+        v = mc < 0 ? static_cast<uint8_t>(j.v_const) : vrow[static_cast<long>(mc) * c + ch];
+      }
+      seg[i] = v;
     }
-    seg[i] = v;
-  }
-  __syncthreads();
-  uint8_t *drow = j.dst + static_cast<int64_t>(y) * j.dst_stride;
-  for (int k = 0; k < 4; ++k) {
-    const int local = threadIdx.x * 4 + k;
-    const long x = x0 + local;
-    if (x >= wc) break;
-    uint32_t acc = 0;
-    for (int t = 0; t < j.ksize; ++t) acc += weight(j, t) * seg[local + t * c];
-    drow[x] = static_cast<uint8_t>(h_saturates(j, x, wc) ? round_sat(acc) : round_wrap(acc));
+    __syncthreads();
+    uint8_t *drow = j.dst + static_cast<int64_t>(y) * j.dst_stride;
+    for (int k = 0; k < 4; ++k) {
+      const int local = threadIdx.x * 4 + k;
+      const long x = x0 + local;
+      if (x >= wc) break;
+      uint32_t acc = 0;
+      for (int t = 0; t < j.ksize; ++t) acc += weight(j, t) * seg[local + t * c];
+      if (right_quirk && x >= wc - j.arb_border_len) {
+        const uint8_t *last = vrow + wc - c;
+        for (int d = 1; d <= r; ++d) {
+          const int qc = right_lane_channel(x, d, c, wc, j.arb_border_len);
+          if (qc >= 0) acc = acc - weight(j, r + d) * seg[local + (r + d) * c] + weight(j, r + d) * last[qc];
+        }
+      }
+      drow[x] = static_cast<uint8_t>(h_saturates(j, x, wc) ? round_sat(acc) : round_wrap(acc));
+    }
   }
 }
 
@@ -123,13 +156,14 @@ cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch, siz
                                     cudaStream_t stream) {
   const long wc = static_cast<long>(job.width) * job.channels;
   const long words = (wc + 3) / 4;
-  dim3 g1(static_cast<unsigned>((words + 255) / 256),
-          static_cast<unsigned>((job.height + kRowsPerThread - 1) / kRowsPerThread));
+  const long row_blocks = (job.height + kRowsPerThread - 1) / kRowsPerThread;
+  dim3 g1(static_cast<unsigned>((words + 255) / 256), static_cast<unsigned>(row_blocks < 65535 ? row_blocks : 65535));
   generic_vertical<<<g1, 256, 0, stream>>>(job, scratch, scratch_stride);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const size_t smem = kHElems + 2 * static_cast<size_t>(job.ksize / 2) * job.channels;
-  dim3 g2(static_cast<unsigned>((wc + kHElems - 1) / kHElems), static_cast<unsigned>(job.height));
+  dim3 g2(static_cast<unsigned>((wc + kHElems - 1) / kHElems),
+          static_cast<unsigned>(job.height < 65535 ? job.height : 65535));
   generic_horizontal<<<g2, kHThreads, smem, stream>>>(job, scratch, scratch_stride);
   return cudaGetLastError();
 }

@@ -113,18 +113,21 @@ __global__ void __launch_bounds__(128) median_small_kernel(const uint8_t *src, i
   int cidx[K];
 #pragma unroll
   for (int d = 0; d < K; ++d) cidx[d] = map_index(col + d - R, w, border) * c + ch;
-  const int y0 = blockIdx.y * rows_per_block, y1 = min(h, y0 + rows_per_block);
-  for (int y = y0; y < y1; ++y) {
-    uint32_t a[K * K];
+  // Row blocks loop over the grid's y extent, which the hardware caps at 65535.
+  for (long yb = blockIdx.y; yb * rows_per_block < h; yb += gridDim.y) {
+    const int y0 = static_cast<int>(yb * rows_per_block), y1 = min(h, y0 + rows_per_block);
+    for (int y = y0; y < y1; ++y) {
+      uint32_t a[K * K];
 #pragma unroll
-    for (int dy = 0; dy < K; ++dy) {
-      const T *row = reinterpret_cast<const T *>(
-          src + static_cast<int64_t>(map_index(y + dy - R, h, border)) * src_stride);
+      for (int dy = 0; dy < K; ++dy) {
+        const T *row = reinterpret_cast<const T *>(
+            src + static_cast<int64_t>(map_index(y + dy - R, h, border)) * src_stride);
 #pragma unroll
-      for (int dx = 0; dx < K; ++dx) a[dy * K + dx] = Key<T>::to(__ldg(row + cidx[dx]));
+        for (int dx = 0; dx < K; ++dx) a[dy * K + dx] = Key<T>::to(__ldg(row + cidx[dx]));
+      }
+      reinterpret_cast<T *>(dst + static_cast<int64_t>(y) * dst_stride)[xe] =
+          Key<T>::from(forgetful<K * K>(a));
     }
-    reinterpret_cast<T *>(dst + static_cast<int64_t>(y) * dst_stride)[xe] =
-        Key<T>::from(forgetful<K * K>(a));
   }
 }
 
@@ -143,43 +146,46 @@ __global__ void __launch_bounds__(kHistThreads) median_hist_kernel(const uint8_t
                                                                   int border, int run) {
   __shared__ uint16_t hist[256 * kHistThreads];  // [bin][thread]; counts <= 255 * 255
   const int tid = threadIdx.x;
-  const int g = blockIdx.x * kHistThreads + tid;  // (segment, channel) item of row y
-  const int y = blockIdx.y;
+  const int g = blockIdx.x * kHistThreads + tid;  // (segment, channel) item of a row
   const int ch = g % c, seg = g / c;
   const int x0 = seg * run;
   if (x0 >= w) return;  // no __syncthreads below: threads are independent
   const int x1 = min(w, x0 + run);
   const int r = k / 2;
   const int m = (k * k - 1) / 2;  // rank of the median
-  for (int b = 0; b < 256; ++b) hist[b * kHistThreads + tid] = 0;
   auto value = [&](int yy, int xx) -> int {
     const uint8_t *row = src + static_cast<int64_t>(map_index(yy, h, border)) * src_stride;
     return __ldg(row + map_index(xx, w, border) * c + ch);
   };
-  for (int dy = -r; dy <= r; ++dy)
-    for (int dx = -r; dx <= r; ++dx) ++hist[value(y + dy, x0 + dx) * kHistThreads + tid];
-  int med = 0, lt = 0;
-  while (lt + hist[med * kHistThreads + tid] <= m) lt += hist[(med++) * kHistThreads + tid];
-  uint8_t *drow = dst + static_cast<int64_t>(y) * dst_stride;
-  drow[x0 * c + ch] = static_cast<uint8_t>(med);
-  for (int x = x0 + 1; x < x1; ++x) {
-    for (int dy = -r; dy <= r; ++dy) {
-      const int out = value(y + dy, x - 1 - r), in = value(y + dy, x + r);
-      --hist[out * kHistThreads + tid];
-      ++hist[in * kHistThreads + tid];
-      lt += (in < med) - (out < med);
-    }
-    while (lt > m) lt -= hist[(--med) * kHistThreads + tid];
+  // Rows loop over the grid's y extent, which the hardware caps at 65535.
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    for (int b = 0; b < 256; ++b) hist[b * kHistThreads + tid] = 0;
+    for (int dy = -r; dy <= r; ++dy)
+      for (int dx = -r; dx <= r; ++dx) ++hist[value(y + dy, x0 + dx) * kHistThreads + tid];
+    int med = 0, lt = 0;
     while (lt + hist[med * kHistThreads + tid] <= m) lt += hist[(med++) * kHistThreads + tid];
-    drow[x * c + ch] = static_cast<uint8_t>(med);
+    uint8_t *drow = dst + static_cast<int64_t>(y) * dst_stride;
+    drow[x0 * c + ch] = static_cast<uint8_t>(med);
+    for (int x = x0 + 1; x < x1; ++x) {
+      for (int dy = -r; dy <= r; ++dy) {
+        const int out = value(y + dy, x - 1 - r), in = value(y + dy, x + r);
+        --hist[out * kHistThreads + tid];
+        ++hist[in * kHistThreads + tid];
+        lt += (in < med) - (out < med);
+      }
+      while (lt > m) lt -= hist[(--med) * kHistThreads + tid];
+      while (lt + hist[med * kHistThreads + tid] <= m) lt += hist[(med++) * kHistThreads + tid];
+      drow[x * c + ch] = static_cast<uint8_t>(med);
+    }
   }
 }
 
 template <typename T, int K>
 cudaError_t launch_small(const MedianJob &j, cudaStream_t s) {
   const int rows_per_block = 4;
+  const int row_blocks = (j.height + rows_per_block - 1) / rows_per_block;
   dim3 grid(static_cast<unsigned>((j.width * j.channels + 127) / 128),
-            static_cast<unsigned>((j.height + rows_per_block - 1) / rows_per_block));
+            static_cast<unsigned>(row_blocks < 65535 ? row_blocks : 65535));
   median_small_kernel<T, K><<<grid, 128, 0, s>>>(j.src, j.src_stride, j.dst, j.dst_stride,
                                                   j.width, j.height, j.channels, j.border,
                                                   rows_per_block);
@@ -204,7 +210,7 @@ cudaError_t launch_median(const MedianJob &j, cudaStream_t s) {
     const int run = hist_run(j.ksize);
     const int items = j.channels * ((j.width + run - 1) / run);
     dim3 grid(static_cast<unsigned>((items + kHistThreads - 1) / kHistThreads),
-              static_cast<unsigned>(j.height));
+              static_cast<unsigned>(j.height < 65535 ? j.height : 65535));
     median_hist_kernel<<<grid, kHistThreads, 0, s>>>(j.src, j.src_stride, j.dst, j.dst_stride,
                                                      j.width, j.height, j.channels, j.ksize,
                                                      j.border, run);
