@@ -145,12 +145,81 @@ def test_oracle_sigma_within_one_of_mask_product(oracle, k, sigma):
         w = k + 9 if k <= 21 else (((k // 2) + 7) // 8 * 8 + k // 2 + 5)
         h = k + 2
         img = rng.integers(0, 256, (h, w * channels), dtype=np.uint8)
-        borders = [1, 2, 3, 4] if k in (3, 5, 7, 9, 15, 21) else [1]
+        fixed = k in (3, 5, 7, 9, 15, 21)
+        borders = [1, 2, 3, 4] if fixed else [1]
+        # The arbitrary-size path's right-border vectors take some replicated
+        # lanes from another channel of the last pixel when channels > 1
+        # (pinned separately below): compare only the columns before them.
+        cols = w * channels if fixed or channels == 1 else w * channels - ((channels * (k // 2) + 7) // 8 * 8)
         for border in borders:
             err, dst = oracle.gaussian_blur_u8(img, w, h, channels, k, sigma, border)
             assert err == 0
             want = (_mask_conv(img, w, channels, full, full, border) + 32768) >> 16
-            assert np.abs(dst.astype(np.int64) - want).max() <= 1
+            assert np.abs(dst.astype(np.int64) - want)[:, :cols].max() <= 1
+
+
+def _right_lane_sources(c, w, k):
+    """Element index each right-border vector lane of the reference's
+    arbitrary-size horizontal pass reads, per (output element, tap distance),
+    restated from the index vectors of its GenericBorderHorizontal
+    (kleidicv/src/filters/border_generic_neon.h:22-98) and the lane loop of
+    horizontal_right_border_vector_path (gaussian_blur_arbitrary_neon.cpp:346-377)."""
+    mask = (1 << 64) - 1
+    data_idx = sum(i << (8 * i) for i in range(8))
+    right = 0
+    for i in range(8):
+        right = ((right << 8) | (((7 - i) % c) + 8 - c)) & mask
+    wc, r = w * c, k // 2
+    border_len = (c * r + 7) // 8 * 8
+    out = {}
+    for xv in range(wc - border_len, wc, 8):
+        for i in range(r):  # pair i: right tap at distance r - i columns
+            start = xv + c * (r - i)
+            if start <= wc - 8:
+                continue
+            shift = 8 * (start - (wc - 8))
+            if shift < 64:
+                idx = ((data_idx >> shift) | (right << (64 - shift))) & mask
+            else:
+                shift = ((start - wc) % c) * 8
+                idx = right if shift == 0 else \
+                    ((((right >> (8 * c - shift)) << (64 - shift)) | (right >> shift)) & mask)
+            for lane in range(8):
+                out[(xv + lane, r - i)] = wc - 8 + ((idx >> (8 * lane)) & 0xFF)
+    return out
+
+
+@pytest.mark.parametrize("c", [2, 3, 4])
+@pytest.mark.parametrize("k,sigma", [(11, 0.0), (13, 2.2), (23, 4.0), (31, 0.0)])
+def test_oracle_arbitrary_right_border_lanes(oracle, c, k, sigma):
+    """The arbitrary-size Gaussian's last elements of every row, against a
+    direct model of the reference's vector lanes: the horizontal pass over the
+    vertical result, with each right-hand tap read where the reference's index
+    vector points."""
+    rng = np.random.default_rng(k * 10 + c)
+    r = k // 2
+    w = (r + 7) // 8 * 8 + r + 5
+    h = k + 1
+    img = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+    err, dst = oracle.gaussian_blur_u8(img, w, h, c, k, sigma, 1)
+    assert err == 0
+    hk = oracle.half_kernel(k, sigma)
+    g = np.array(hk + hk[-2::-1], np.int64)
+    # vertical pass (u8 intermediate, REPLICATE rows), as the reference computes it
+    rows = np.clip(np.arange(h)[:, None] + np.arange(-r, r + 1)[None, :], 0, h - 1)
+    vert = ((img.astype(np.int64)[rows] * g[None, :, None]).sum(axis=1) + 128) >> 8
+    src = _right_lane_sources(c, w, k)
+    wc = w * c
+    border_len = (c * r + 7) // 8 * 8
+    for x in range(wc - border_len, wc):
+        col, ch = divmod(x, c)
+        acc = g[r] * vert[:, x]
+        for d in range(1, r + 1):
+            left = vert[:, max(col - d, 0) * c + ch]
+            rgt = vert[:, src[(x, d)]] if (x, d) in src else vert[:, min(col + d, w - 1) * c + ch]
+            acc = acc + g[r - d] * (left + rgt)
+        want = (acc + 128) >> 8
+        assert np.array_equal(dst[:, x], want & 0xFF), f"element {x}"
 
 
 @pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
