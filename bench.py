@@ -68,7 +68,14 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="c1,batched,pyramid,lk_pyramid,sobel,median,thread_api,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
-    ap.add_argument("--serving-seconds", type=float, default=3.0)
+    ap.add_argument("--profile-op", choices=("gauss", "u16", "s16", "blurdown", "sobel"), default=None,
+                    help="run one workload 3 times on cuda:0 and exit (a small command for profiler captures): "
+                         "the sweep's Gaussian / u16 REFLECT / s16 REFLECT call, blur_and_downsample_u8 of a "
+                         "4096x4096x1 image, or the d/dx Sobel of a 3840x2160x1 image")
+    ap.add_argument("--serving-seconds", type=float, default=60.0)
+    ap.add_argument("--serving-high-seconds", type=float, default=10.0)
+    ap.add_argument("--serving-inflight", type=int, default=3)
+    ap.add_argument("--serving-batch-mb", type=int, default=0, help="work budget per batch in MiB (0: none)")
     ap.add_argument("--serving-rate", type=float, default=2000.0)
     return ap.parse_args()
 
@@ -887,16 +894,22 @@ def section_pyramid(torch, kcv, ctx, stream):
     return out
 
 
-def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
+def section_serving(torch, kcv, seconds, rate, high_seconds=10.0, inflight=3, batch_requests=512,
+                    batch_mb=0):
     """Seed 4: Poisson arrivals at `rate` requests/s for `seconds`; 0.60
     gaussian_blur_u8 / 0.25 separable_filter_2d_u16 / 0.15
     blur_and_downsample_u8; w 320-7680, h 240-4320 log-uniform, C {1,3,4},
     Gaussian k {3,5,7,15}, separable 5x5, random border; images resident in the
     server's 40 GB pool.  Requests draw from 48 resident source images of those
     shapes, each with a ring of 16 output buffers (a buffer is reused 16
-    requests of its image later, long after that request completed)."""
+    requests of its image later, long after that request completed).  Every
+    500th request of each run writes to a buffer of its own instead, and those
+    outputs are compared byte for byte with the CPU oracle after the run."""
+    from oracle import oracle
+
     rng = np.random.default_rng(4)
-    srv = kcv.Server(0, pool_limit_bytes=40 << 30, max_inflight_batches=inflight, max_batch_requests=batch_requests)
+    srv = kcv.Server(0, pool_limit_bytes=40 << 30, max_inflight_batches=inflight, max_batch_requests=batch_requests,
+                     max_batch_bytes=batch_mb << 20)
     templates = []
     for _ in range(48):
         u = rng.random()
@@ -910,18 +923,20 @@ def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
         staging = torch.from_numpy(host.view(np.uint8).reshape(-1)).cuda()
         _copy_device(ptr, staging.data_ptr(), host.nbytes)
         del staging
-        tp = dict(op=op, w=w, h=h, c=c, dtype=dtype, src=ptr, next=0)
+        tp = dict(op=op, w=w, h=h, c=c, dtype=dtype, src=ptr, next=0, host=host)
         ow, oh = ((w + 1) // 2, (h + 1) // 2) if op == "bd" else (w, h)
         tp["mpix"] = ow * oh / 1e6
-        tp["ring"] = [srv.alloc(ow * oh * c * np.dtype(dtype).itemsize) for _ in range(16)]
+        tp["out_bytes"] = ow * oh * c * np.dtype(dtype).itemsize
+        tp["ring"] = [srv.alloc(tp["out_bytes"]) for _ in range(16)]
         assert all(tp["ring"]), "pool exhausted"
         templates.append(tp)
     torch.cuda.synchronize()
 
-    def make_req(tp):
+    def make_req(tp, dst=None):
         es = np.dtype(tp["dtype"]).itemsize
-        dst = tp["ring"][tp["next"] % 16]
-        tp["next"] += 1
+        if dst is None:
+            dst = tp["ring"][tp["next"] % 16]
+            tp["next"] += 1
         border = int(rng.choice([1, 2, 3, 4]))
         if tp["op"] == "gauss":
             k = int(rng.choice([3, 5, 7, 15]))
@@ -937,13 +952,27 @@ def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
         return kcv.make_request(kcv.OP_BLUR_AND_DOWNSAMPLE_U8, tp["src"], tp["w"] * tp["c"], dst, ow * tp["c"],
                                 tp["w"], tp["h"], tp["c"], border_type=border)
 
+    checked = []  # (template, request, own output buffer)
+    cap = [30]    # checked requests per run
+
     def build(n, r):
         arrivals = np.cumsum(rng.exponential(1.0 / r, n))
         picks = rng.integers(0, len(templates), n)
-        return arrivals, [(templates[t], make_req(templates[t])) for t in picks]
+        reqs = []
+        for k, t in enumerate(picks):
+            tp = templates[t]
+            if k % 500 == 250 and len(checked) < cap[0]:
+                own = srv.alloc(tp["out_bytes"])
+                if own:
+                    req = make_req(tp, own)
+                    checked.append((tp, req, own))
+                    reqs.append((tp, req))
+                    continue
+            reqs.append((tp, make_req(tp)))
+        return arrivals, reqs
 
     def drive(arrivals, reqs):
-        pending, lat, mpix, busy = {}, [], 0.0, 0
+        pending, lat, qlat, mpix, busy, failed = {}, [], [], 0.0, 0, 0
         n, i = len(reqs), 0
         t_start = time.perf_counter()
         while i < n or pending:
@@ -957,19 +986,27 @@ def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
                 i += 1
             for rid, st, ta, tad, tc in srv.poll(256, timeout_ms=0):
                 tp = pending.pop(rid)
+                failed += st != kcv.OK
                 lat.append((tc - ta) * 1e3)
+                qlat.append((tad - ta) * 1e3)
                 mpix += tp["mpix"]
             if i < n and not pending:
                 time.sleep(max(0.0, min(arrivals[i] - (time.perf_counter() - t_start), 0.0005)))
         wall = time.perf_counter() - t_start
-        lat = np.array(lat)
-        return {"requests": n, "completed": int(len(lat)), "busy": busy,
-                "offered_req_s": round(n / arrivals[-1], 1), "mpix_s": round(mpix / wall, 1),
+        lat, qlat = np.array(lat), np.array(qlat)
+        return {"queue_p50_ms": round(float(np.percentile(qlat, 50)), 3),
+                "queue_p99_ms": round(float(np.percentile(qlat, 99)), 3),
+                "requests": n, "completed": int(len(lat)), "busy": busy, "failed": int(failed),
+                "seconds": round(wall, 2), "offered_req_s": round(n / arrivals[-1], 1),
+                "mpix_s": round(mpix / wall, 1),
                 "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
                 "p999_ms": round(float(np.percentile(lat, 99.9)), 3)}
 
+    warm_arr, warm_reqs = build(200, rate)
+    drive(warm_arr - warm_arr[0], warm_reqs)  # warm-up
+    checked.clear()
     arrivals, reqs = build(int(seconds * rate), rate)
-    drive(arrivals[:200] - arrivals[0], reqs[:200])  # warm-up
+    n_main_checked = len(checked)
     main_run = drive(arrivals, reqs)
     srv.drain()
     # The first 1000 requests as plain per-request calls back to back and as one batch plan.
@@ -990,22 +1027,58 @@ def section_serving(torch, kcv, seconds, rate, inflight=3, batch_requests=512):
     batch_ms = _events_time(torch, stream, lambda _: plan.launch(True), 3)
     plan.close()
     batched_mpix_s = sample_mpix / (batch_ms * 1e-3)
+    # The plain calls and the batch above rewrote the checked outputs with the
+    # same bytes; the comparison below covers the served results regardless.
     # Sustained load at 80% of the batched throughput.
     mean_mpix = float(np.mean([tp["mpix"] for tp, _ in reqs]))
     high_rate = 0.8 * batched_mpix_s / mean_mpix
-    arr_h, reqs_h = build(int(1.5 * high_rate), high_rate)
+    cap[0] = len(checked) + 30
+    arr_h, reqs_h = build(int(high_seconds * high_rate), high_rate)
     high_run = drive(arr_h, reqs_h)
     srv.drain()
     ctx.close()
+    # Served outputs against the CPU oracle, byte for byte.
+    exact, n_checked = True, 0
+    for tp, r, own in checked:
+        got = np.empty(tp["out_bytes"], np.uint8)
+        _copy_to_host(got, own)
+        if tp["op"] == "gauss":
+            e, want = oracle.gaussian_blur_u8(tp["host"], tp["w"], tp["h"], tp["c"], r.kernel_width, r.sigma_x,
+                                              r.border_type, nthreads=os.cpu_count() or 1)
+        elif tp["op"] == "sep":
+            e, want = oracle.separable_filter_2d(tp["host"], tp["w"], tp["h"], tp["c"],
+                                                 np.array(list(r.kernel_x)[:5], np.uint16),
+                                                 np.array(list(r.kernel_y)[:5], np.uint16), r.border_type,
+                                                 nthreads=os.cpu_count() or 1)
+        else:
+            e, want = oracle.blur_and_downsample_u8(tp["host"], tp["w"], tp["h"], tp["c"], r.border_type,
+                                                    nthreads=os.cpu_count() or 1)
+        exact &= e == 0 and np.array_equal(got, np.ascontiguousarray(want).view(np.uint8).reshape(-1))
+        n_checked += 1
     srv.close()
     out = {"config": f"Poisson {rate:.0f} req/s for {seconds:.1f} s (seed 4), mix 0.60/0.25/0.15, "
                      "w 320-7680 h 240-4320 log-uniform, 48 resident source images, 40 GB pool, "
-                     f"{inflight} batches in flight, <= {batch_requests} requests per batch"}
+                     f"{inflight} batches in flight, <= {batch_requests} requests"
+                     + (f" and <= {batch_mb} MiB of image traffic" if batch_mb else "") + " per batch"}
     out.update(main_run)
     out.update({"plain_per_request_mpix_s": round(sample_mpix / (plain_ms * 1e-3), 1),
                 "batched_mpix_s": round(batched_mpix_s, 1), "comparison_sample": f"first {len(sample)} requests",
-                "load_80pct_of_batched": high_run})
+                "load_80pct_of_batched": high_run,
+                "served_bit_exact": bool(exact), "served_checked": n_checked,
+                "served_check": f"every 500th request of each run (at most 30 per run; {n_main_checked} in the "
+                                "configured run), own output buffer, against the CPU oracle"})
     return out
+
+
+def _copy_to_host(host_array, src_ptr):
+    """Device bytes at a raw pointer -> a host numpy array (cudaMemcpy through ctypes)."""
+    import ctypes
+
+    lib = _cudart()
+    lib.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    err = lib.cudaMemcpy(ctypes.c_void_p(host_array.ctypes.data), ctypes.c_void_p(src_ptr),
+                         ctypes.c_size_t(host_array.nbytes), 2)
+    assert err == 0, err
 
 
 def _with_dst(kcv, r, dst):
@@ -1086,7 +1159,9 @@ def run_sections(args, names):
             elif name == "sobel":
                 out[name] = section_sobel(torch, kcv, ctx, stream, cores)
             elif name == "serving":
-                out[name] = section_serving(torch, kcv, args.serving_seconds, args.serving_rate)
+                out[name] = section_serving(torch, kcv, args.serving_seconds, args.serving_rate,
+                                            args.serving_high_seconds, args.serving_inflight,
+                                            batch_mb=args.serving_batch_mb)
         except Exception as e:  # a failed section must not lose the headline line
             out[name] = {"error": f"{type(e).__name__}: {e}"}
         out[name]["section_seconds"] = round(time.perf_counter() - t0, 1)
@@ -1154,8 +1229,49 @@ def reference_arm(args, calls, config):
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def profile_op(name):
+    """One workload, three calls, for a profiler capture (`--profile-op`)."""
+    import torch
+    import __graft_entry__ as ge
+
+    kcv = ge.package()
+    ctx = kcv.Context.for_torch(0)
+    calls, _ = make_calls()
+    rng = np.random.default_rng(3)
+    if name in ("gauss", "u16", "s16"):
+        c = {"gauss": calls[0], "u16": calls[1], "s16": calls[4]}[name]
+        src = torch.from_numpy(c["src"].view(np.uint8)).cuda()
+        dst = torch.empty_like(src)
+        ss = src.stride(0)
+        if name == "gauss":
+            f = lambda: kcv.gaussian_blur_u8(src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 4, 7, 7, 1.5, 1.5,  # noqa
+                                             c["border"], ctx)
+        else:
+            f = lambda: kcv.separable_filter_2d(c["dtype"], src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 1,  # noqa
+                                                c["kx"], 5, c["ky"], 5, c["border"], ctx, border_value=c["bv"])
+    elif name == "blurdown":
+        src = torch.from_numpy(_pyr_image(rng, 4096, 4096, 1)).cuda()
+        dst = torch.empty((2048, 2048), dtype=torch.uint8, device="cuda")
+        f = lambda: kcv.blur_and_downsample_u8(src.data_ptr(), 4096, 4096, 4096, dst.data_ptr(), 2048, 1,  # noqa
+                                               kcv.REVERSE, ctx)
+    else:
+        src = torch.from_numpy(rng.integers(0, 256, (H, W), dtype=np.uint8)).cuda()
+        dst = torch.empty((H, W), dtype=torch.int16, device="cuda")
+        f = lambda: kcv.sobel_3x3_horizontal_s16_u8(src.data_ptr(), W, dst.data_ptr(), 2 * W, W, H, 1, ctx)  # noqa
+    for _ in range(3):
+        if f() != kcv.OK:
+            raise RuntimeError(f"{name} call failed")
+    if ctx.synchronize() != kcv.OK:
+        raise RuntimeError(f"{name} failed on the device")
+    ctx.close()
+    print(f"profile-op {name}: 3 calls done", flush=True)
+
+
 def main():
     args = parse_args()
+    if args.profile_op:
+        profile_op(args.profile_op)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     calls, taps = make_calls()

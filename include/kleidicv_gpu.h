@@ -82,6 +82,7 @@ typedef enum {
 #define KLEIDICV_GPU_ERROR_NO_DEVICE ((kleidicv_error_t)0x101) /* no usable sm_103 device */
 #define KLEIDICV_GPU_ERROR_TIMEOUT ((kleidicv_error_t)0x102)   /* a device wait hit its limit */
 #define KLEIDICV_GPU_ERROR_BUSY ((kleidicv_error_t)0x103)      /* serving queue full */
+#define KLEIDICV_GPU_ERROR_NOT_READY ((kleidicv_error_t)0x104) /* asynchronous call still running */
 
 /* KLEIDICV_MAX_IMAGE_PIXELS and KLEIDICV_MAXIMUM_CHANNEL_COUNT, kleidicv.h:103,110 */
 #define KLEIDICV_GPU_MAX_IMAGE_PIXELS ((1ULL << 48) - 1)
@@ -353,6 +354,10 @@ typedef struct {
   int max_inflight_batches;   /* batches allowed on the GPU at once (0 = 3) */
   int max_batch_requests;     /* requests per batch (0 = 512) */
   int max_queue;              /* pending requests before BUSY (0 = 65536) */
+  size_t max_batch_bytes;     /* work budget of one batch: the requests' image
+                                 bytes read plus written; a batch takes the
+                                 oldest requests until the budget is reached,
+                                 at least one (0 = no budget) */
 } kleidicv_gpu_server_config_t;
 
 typedef struct {

@@ -120,6 +120,64 @@ kleidicv_error_t kleidicv_gpu_thread_median_blur_f32(
     size_t channels, size_t kernel_width, size_t kernel_height,
     kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt);
 
+/* ---- Asynchronous variant (no counterpart in the reference) -------------
+ *
+ * The same calls, returning once the work is enqueued instead of once `dst`
+ * holds the result: the scheduler contract of kleidicv_thread.h:42-97 with a
+ * completion callback instead of a blocking return.
+ *
+ *  - Validation is the synchronous call's, in its order; a call that fails it
+ *    enqueues nothing, never calls `done` and sets *handle to NULL.
+ *  - Before returning, the call runs the upload phase through `mt` (packing a
+ *    pageable source into pinned staging) and enqueues the filter and the
+ *    device-to-host copies on the calling thread's default context.
+ *  - A library worker thread of that context then finishes the call: it runs
+ *    the download phase through `mt` (unpacking into a pageable `dst`), frees
+ *    the call's device memory, calls `done(status, user_data)` if `done` is
+ *    not NULL, and marks the handle complete.  The scheduler's `parallel`
+ *    must therefore accept calls from that thread.  Calls made from one
+ *    thread complete in the order they were made.
+ *  - `src` and `dst` must stay valid, and `src` unchanged, until completion.
+ *  - With `handle` non-NULL the caller owns a handle: query it, wait on it and
+ *    release it (release waits for completion).  With `handle` NULL the library
+ *    releases everything itself after `done` returns.
+ */
+typedef struct kleidicv_gpu_async kleidicv_gpu_async_t;
+typedef void (*kleidicv_gpu_async_callback)(kleidicv_error_t status, void *user_data);
+
+kleidicv_error_t kleidicv_gpu_thread_gaussian_blur_u8_async(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height, float sigma_x,
+    float sigma_y, kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt,
+    kleidicv_gpu_async_callback done, void *user_data, kleidicv_gpu_async_t **handle);
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u8_async(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint8_t *kernel_x, size_t kernel_width,
+    const uint8_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle);
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u16_async(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint16_t *kernel_x, size_t kernel_width,
+    const uint16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle);
+
+kleidicv_error_t kleidicv_gpu_thread_blur_and_downsample_u8_async(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height, uint8_t *dst,
+    size_t dst_stride, size_t channels, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle);
+
+/* KLEIDICV_GPU_ERROR_NOT_READY while the call runs, then its final status. */
+kleidicv_error_t kleidicv_gpu_async_query(const kleidicv_gpu_async_t *handle);
+/* Blocks until the call completed; returns its final status. */
+kleidicv_error_t kleidicv_gpu_async_wait(kleidicv_gpu_async_t *handle);
+/* Waits for completion, then frees the handle. */
+kleidicv_error_t kleidicv_gpu_async_release(kleidicv_gpu_async_t *handle);
+
 /* A persistent worker pool implementing kleidicv_thread_parallel: `threads`
  * workers (0: the hardware concurrency) plus the calling thread take task
  * indices one at a time until all are done; the first failing callback's

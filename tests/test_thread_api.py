@@ -142,3 +142,44 @@ def test_threaded_median_validates_like_the_reference(lib, kcv, oracle, no_gpu, 
             assert fn(a.ctypes.data, 64 + 1, b.ctypes.data, 64, 10, 10, 1, 5, 5, 1, pool.mt) == kcv.ALIGNMENT
     finally:
         pool.close()
+
+
+def test_async_entries_validate_synchronously(lib, kcv, no_gpu):
+    """The asynchronous variants: validation errors come back from the call,
+    with no handle and no callback; without a device the call fails loudly;
+    the handle functions reject NULL."""
+    pool = kcv.ThreadPool(2)
+    calls = []
+
+    @kcv.ASYNC_CALLBACK
+    def done(status, user):
+        calls.append(status)
+
+    a = np.zeros((16, 64), np.uint8)
+    b = np.zeros((16, 64), np.uint8)
+    g = lib.kleidicv_gpu_thread_gaussian_blur_u8_async
+    h = ctypes.c_void_p(12345)
+    cb = ctypes.cast(done, ctypes.c_void_p)
+    try:
+        assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 4, 4, 0.0, 0.0, kcv.REFLECT, pool.mt, cb, None,
+                 ctypes.byref(h)) == kcv.NOT_IMPLEMENTED
+        assert h.value is None
+        assert g(None, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT, pool.mt, cb, None,
+                 ctypes.byref(h)) == kcv.NULL_POINTER
+        assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT,
+                 kcv.ThreadMT(None, None), cb, None, ctypes.byref(h)) == kcv.NULL_POINTER
+        assert lib.kleidicv_gpu_thread_separable_filter_2d_u16_async(
+            a.ctypes.data, 63, b.ctypes.data, 64, 32, 16, 1, a.ctypes.data, 5, a.ctypes.data, 5, kcv.REFLECT,
+            pool.mt, cb, None, ctypes.byref(h)) == kcv.ALIGNMENT
+        assert lib.kleidicv_gpu_thread_blur_and_downsample_u8_async(
+            a.ctypes.data, 64, 64, 16, b.ctypes.data, 64, 1, kcv.CONSTANT, pool.mt, cb, None,
+            ctypes.byref(h)) == kcv.NOT_IMPLEMENTED
+        if no_gpu:
+            assert g(a.ctypes.data, 64, b.ctypes.data, 64, 64, 16, 1, 5, 5, 0.0, 0.0, kcv.REFLECT, pool.mt, cb,
+                     None, ctypes.byref(h)) == kcv.ERROR_NO_DEVICE
+            assert h.value is None and not b.any()
+        assert calls == []
+        for fn in ("kleidicv_gpu_async_query", "kleidicv_gpu_async_wait", "kleidicv_gpu_async_release"):
+            assert getattr(lib, fn)(None) == kcv.NULL_POINTER
+    finally:
+        pool.close()

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "libkleidicv_gpu.so")
 
 # kleidicv_error_t (kleidicv/include/kleidicv/ctypes.h:26-41) + GPU extensions
 OK, NOT_IMPLEMENTED, NULL_POINTER, RANGE, ALLOCATION, ALIGNMENT, CONTEXT_MISMATCH = range(7)
-ERROR_CUDA, ERROR_NO_DEVICE, ERROR_TIMEOUT, ERROR_BUSY = 0x100, 0x101, 0x102, 0x103
+ERROR_CUDA, ERROR_NO_DEVICE, ERROR_TIMEOUT, ERROR_BUSY, ERROR_NOT_READY = 0x100, 0x101, 0x102, 0x103, 0x104
 # kleidicv_border_type_t (ctypes.h:60-79)
 CONSTANT, REPLICATE, REFLECT, WRAP, REVERSE, TRANSPARENT, NONE = range(7)
 # kleidicv_gpu_op_t
@@ -28,7 +28,7 @@ OP_GAUSSIAN_BLUR_U8, OP_SEPARABLE_U8, OP_SEPARABLE_U16, OP_SEPARABLE_S16, OP_BLU
 
 ERROR_NAMES = {0: "OK", 1: "NOT_IMPLEMENTED", 2: "NULL_POINTER", 3: "RANGE", 4: "ALLOCATION",
                5: "ALIGNMENT", 6: "CONTEXT_MISMATCH", 0x100: "CUDA", 0x101: "NO_DEVICE",
-               0x102: "TIMEOUT", 0x103: "BUSY"}
+               0x102: "TIMEOUT", 0x103: "BUSY", 0x104: "NOT_READY"}
 
 _sz, _vp, _f, _i, _u8, _u16, _i16 = (ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
                                      ctypes.c_uint8, ctypes.c_uint16, ctypes.c_int16)
@@ -46,7 +46,7 @@ class Request(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("pool_limit_bytes", _sz), ("max_inflight_batches", _i), ("max_batch_requests", _i),
-                ("max_queue", _i)]
+                ("max_queue", _i), ("max_batch_bytes", _sz)]
 
 
 class ThreadMT(ctypes.Structure):
@@ -101,6 +101,18 @@ SIGNATURES = {
     "kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, ThreadMT]),
     **{f"kleidicv_gpu_thread_median_blur_{t}": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _i, ThreadMT])
        for t in ("s8", "u8", "u16", "s16", "u32", "s32", "f32")},
+    # Asynchronous threaded calls: ..., mt, done callback, user data, handle out.
+    "kleidicv_gpu_thread_gaussian_blur_u8_async": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f,
+                                                        _i, ThreadMT, _vp, _vp, ctypes.POINTER(_vp)]),
+    "kleidicv_gpu_thread_separable_filter_2d_u8_async": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp,
+                                                              _sz, _i, ThreadMT, _vp, _vp, ctypes.POINTER(_vp)]),
+    "kleidicv_gpu_thread_separable_filter_2d_u16_async": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _vp, _sz, _vp,
+                                                               _sz, _i, ThreadMT, _vp, _vp, ctypes.POINTER(_vp)]),
+    "kleidicv_gpu_thread_blur_and_downsample_u8_async": (_i, [_vp, _sz, _sz, _sz, _vp, _sz, _sz, _i, ThreadMT,
+                                                              _vp, _vp, ctypes.POINTER(_vp)]),
+    "kleidicv_gpu_async_query": (_i, [_vp]),
+    "kleidicv_gpu_async_wait": (_i, [_vp]),
+    "kleidicv_gpu_async_release": (_i, [_vp]),
     "kleidicv_gpu_thread_pool_create": (_i, [ctypes.POINTER(_vp), ctypes.c_uint]),
     "kleidicv_gpu_thread_pool_destroy": (_i, [_vp]),
     "kleidicv_gpu_thread_pool_parallel": (_i, [_vp, _vp, _vp, ctypes.c_uint]),
@@ -327,6 +339,9 @@ class ThreadPool:
             self.handle = None
 
 
+ASYNC_CALLBACK = ctypes.CFUNCTYPE(None, _i, _vp)
+
+
 def serial_scheduler():
     """A scheduler written in Python: runs every task range on the calling
     thread (the reference's serial fallback).  Keep the returned pair alive
@@ -476,8 +491,8 @@ class Server:
     """kleidicv_gpu_server_t: continuous batching over a capped device pool."""
 
     def __init__(self, device=0, pool_limit_bytes=0, max_inflight_batches=0, max_batch_requests=0,
-                 max_queue=0):
-        cfg = ServerConfig(pool_limit_bytes, max_inflight_batches, max_batch_requests, max_queue)
+                 max_queue=0, max_batch_bytes=0):
+        cfg = ServerConfig(pool_limit_bytes, max_inflight_batches, max_batch_requests, max_queue, max_batch_bytes)
         h = ctypes.c_void_p()
         err = lib().kleidicv_gpu_server_create(ctypes.byref(cfg), device, ctypes.byref(h))
         if err != OK:

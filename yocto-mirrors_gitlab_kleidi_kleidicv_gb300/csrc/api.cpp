@@ -547,6 +547,7 @@ kleidicv_error_t kleidicv_gpu_context_create(kleidicv_gpu_context_t **out, int d
 kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx) {
   if (!ctx) return KLEIDICV_ERROR_NULL_POINTER;
   DeviceGuard guard(ctx->device);
+  shutdown_async(ctx);
   cudaStreamSynchronize(ctx->stream);
   for (cudaStream_t s : ctx->branches) {
     cudaStreamSynchronize(s);

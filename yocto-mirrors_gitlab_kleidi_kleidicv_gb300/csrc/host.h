@@ -6,12 +6,18 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <condition_variable>
+#include <deque>
 #include <mutex>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/kleidicv_gpu.h"
 #include "kcv_job.h"
 #include "launch.h"
+
+struct kleidicv_gpu_async;
 
 struct kleidicv_gpu_context {
   int device = 0;
@@ -37,6 +43,17 @@ struct kleidicv_gpu_context {
   // grow-only, freed with the context.
   void *pinned = nullptr;
   size_t pinned_bytes = 0;
+  // Asynchronous threaded-API calls (kleidicv_gpu_thread_*_async): pinned
+  // staging buffers kept for reuse, and the completion worker that finishes
+  // queued calls in submission order (started on first use, joined by
+  // kleidicv_gpu_context_destroy).
+  std::mutex pinned_pool_mutex;
+  std::vector<std::pair<void *, size_t>> pinned_pool;
+  std::mutex async_mutex;
+  std::condition_variable async_cv;
+  std::deque<kleidicv_gpu_async *> async_queue;
+  std::thread async_worker;
+  bool async_stop = false;
 };
 
 namespace kcv {
@@ -103,6 +120,10 @@ void encode_tma(FilterJob &j);
 
 // Enqueues a prepared request on ctx's stream.
 kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p);
+
+// Finishes the context's asynchronous threaded calls and stops its
+// completion worker (context destruction).
+void shutdown_async(kleidicv_gpu_context *ctx);
 
 // Context helpers.
 kleidicv_error_t resolve_context(kleidicv_gpu_context *&ctx);

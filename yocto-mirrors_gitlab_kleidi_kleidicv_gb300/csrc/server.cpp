@@ -4,8 +4,8 @@
 // requests at any time and poll completions.  Up to max_inflight_batches
 // batches are on the GPU at once, one per slot (a worker thread with its own
 // stream): a free worker admits the oldest queued requests (up to
-// max_batch_requests, and only as many as the pool's free bytes cover for the
-// batch's own device memory), builds a batch plan for them and launches it
+// max_batch_requests and max_batch_bytes of image traffic, and only as many
+// as the pool's free bytes cover for the batch's own device memory), builds a batch plan for them and launches it
 // while the other slots' batches keep running.  Completion is detected with an
 // event; its requests complete with the server-clock times of arrival,
 // admission and completion.
@@ -57,6 +57,18 @@ size_t batch_bytes(const std::vector<Pending> &reqs) {
   return b;
 }
 
+// The request's image bytes read plus written: the unit of a batch's work
+// budget (its GPU time is close to proportional to it).
+size_t request_bytes(const kleidicv_gpu_request_t &r) {
+  const size_t es =
+      (r.op == KLEIDICV_GPU_OP_SEPARABLE_FILTER_2D_U16 || r.op == KLEIDICV_GPU_OP_SEPARABLE_FILTER_2D_S16) ? 2 : 1;
+  const size_t in = r.width * r.height * r.channels * es;
+  const size_t out = r.op == KLEIDICV_GPU_OP_BLUR_AND_DOWNSAMPLE_U8
+                         ? ((r.width + 1) / 2) * ((r.height + 1) / 2) * r.channels
+                         : in;
+  return in + out;
+}
+
 }  // namespace
 
 struct kleidicv_gpu_server {
@@ -81,11 +93,18 @@ struct kleidicv_gpu_server {
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
-  // Takes the oldest queued requests that the pool's free bytes cover (holds mu).
+  // Takes the oldest queued requests that the pool's free bytes cover, up to
+  // the batch work budget (at least one request) (holds mu).  Bounding a
+  // batch's work bounds how long its requests, and the requests queued behind
+  // it, wait for the GPU.
   std::vector<Pending> take_batch(size_t *need) {
     std::vector<Pending> batch;
     *need = 0;
+    size_t work = 0;
     while (!queue.empty() && batch.size() < static_cast<size_t>(cfg.max_batch_requests)) {
+      const size_t w = request_bytes(queue.front().req);
+      if (!batch.empty() && work + w > cfg.max_batch_bytes) break;
+      work += w;
       batch.push_back(queue.front());
       const size_t n = batch_bytes(batch);
       if (pool_used + n > cfg.pool_limit_bytes && batch.size() > 1) {
@@ -177,6 +196,7 @@ kleidicv_error_t kleidicv_gpu_server_create(const kleidicv_gpu_server_config_t *
   if (cfg.max_inflight_batches <= 0) cfg.max_inflight_batches = 3;
   if (cfg.max_batch_requests <= 0) cfg.max_batch_requests = 512;
   if (cfg.max_queue <= 0) cfg.max_queue = 65536;
+  if (!cfg.max_batch_bytes) cfg.max_batch_bytes = ~static_cast<size_t>(0);
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
     cudaGetLastError();

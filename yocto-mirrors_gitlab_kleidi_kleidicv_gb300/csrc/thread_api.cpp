@@ -176,18 +176,61 @@ kleidicv_error_t download_task(unsigned begin, unsigned end, void *data) {
 using DeviceOp = std::function<kleidicv_error_t(const void *, size_t, void *, size_t,
                                                 kleidicv_gpu_context_t *)>;
 
-kleidicv_error_t run_threaded(kleidicv_error_t validation, const Prepared &p, HostImage src,
-                              HostImage dst, const DeviceOp &op,
-                              kleidicv_thread_multithreading mt) {
-  if (validation != KLEIDICV_OK) return validation;
-  if (!mt.parallel) return KLEIDICV_ERROR_NULL_POINTER;
-  if (p.kind == Prepared::NOTHING) return KLEIDICV_OK;
-  kleidicv_gpu_context_t *ctx = nullptr;
-  kleidicv_error_t e = kcv::resolve_context(ctx);
-  if (e != KLEIDICV_OK) return e;
-  kcv::DeviceGuard guard(ctx->device);
+// Pinned staging of asynchronous calls: buffers from the context's pool
+// (reused), so that calls in flight never share staging.
+void *pool_pinned(kleidicv_gpu_context_t *ctx, size_t bytes, size_t *got) {
+  {
+    std::lock_guard<std::mutex> l(ctx->pinned_pool_mutex);
+    size_t best = ctx->pinned_pool.size();
+    for (size_t i = 0; i < ctx->pinned_pool.size(); ++i)
+      if (ctx->pinned_pool[i].second >= bytes &&
+          (best == ctx->pinned_pool.size() || ctx->pinned_pool[i].second < ctx->pinned_pool[best].second))
+        best = i;
+    if (best < ctx->pinned_pool.size()) {
+      auto b = ctx->pinned_pool[best];
+      ctx->pinned_pool.erase(ctx->pinned_pool.begin() + best);
+      *got = b.second;
+      return b.first;
+    }
+  }
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  *got = bytes;
+  return p;
+}
 
+void pool_return(kleidicv_gpu_context_t *ctx, void *p, size_t bytes) {
+  if (!p) return;
+  std::lock_guard<std::mutex> l(ctx->pinned_pool_mutex);
+  ctx->pinned_pool.emplace_back(p, bytes);
+}
+
+// One threaded call.  begin() validates the sides, runs the upload phase
+// through the scheduler, enqueues the filter and the download copies (one
+// copy and one event per destination stripe); complete() runs the download
+// phase through the scheduler and releases the call's resources.  A
+// synchronous call runs both on the caller's thread; an asynchronous one
+// runs complete() on the context's completion worker.
+struct ThreadedCall {
+  kleidicv_gpu_context_t *ctx = nullptr;
+  kleidicv_thread_multithreading mt{};
+  bool async = false;
   Side s, d;
+  std::vector<cudaEvent_t> events;
+  cudaEvent_t done_event = nullptr;  // async: after the call's last copy
+  void *staging = nullptr;           // async: pinned staging from the pool
+  size_t staging_bytes = 0;
+
+  kleidicv_error_t begin(const Prepared &p, HostImage src, HostImage dst, const DeviceOp &op);
+  kleidicv_error_t complete(kleidicv_error_t result);
+};
+
+kleidicv_error_t ThreadedCall::begin(const Prepared &p, HostImage src, HostImage dst,
+                                     const DeviceOp &op) {
+  kcv::DeviceGuard guard(ctx->device);
   s.img = src;
   d.img = dst;
   // A single-row image may come with any stride (the reference ignores it).
@@ -209,59 +252,179 @@ kleidicv_error_t run_threaded(kleidicv_error_t validation, const Prepared &p, Ho
   const size_t stage_s = (!s.on_device && !s.pinned) ? s.pitch * s.img.rows : 0;
   const size_t stage_d = (!d.on_device && !d.pinned) ? d.pitch * d.img.rows : 0;
   if (stage_s + stage_d > 0) {
-    if (!pinned_staging(ctx, stage_s + stage_d)) return KLEIDICV_ERROR_ALLOCATION;
-    s.stage = static_cast<uint8_t *>(ctx->pinned);
-    d.stage = static_cast<uint8_t *>(ctx->pinned) + stage_s;
+    uint8_t *base;
+    if (async) {
+      staging = pool_pinned(ctx, stage_s + stage_d, &staging_bytes);
+      if (!staging) return KLEIDICV_ERROR_ALLOCATION;
+      base = static_cast<uint8_t *>(staging);
+    } else {
+      if (!pinned_staging(ctx, stage_s + stage_d)) return KLEIDICV_ERROR_ALLOCATION;
+      base = static_cast<uint8_t *>(ctx->pinned);
+    }
+    s.stage = base;
+    d.stage = base + stage_s;
   }
   if (s.dev_bytes) s.dev = static_cast<uint8_t *>(kcv::ctx_alloc(ctx, s.dev_bytes));
   if (d.dev_bytes) d.dev = static_cast<uint8_t *>(kcv::ctx_alloc(ctx, d.dev_bytes));
-  std::vector<cudaEvent_t> events;
-  auto finish = [&](kleidicv_error_t result) {
-    if (!s.on_device) kcv::ctx_free(ctx, s.dev, s.dev_bytes);
-    if (!d.on_device) kcv::ctx_free(ctx, d.dev, d.dev_bytes);
-    const kleidicv_error_t se = kleidicv_gpu_context_synchronize(ctx);
-    for (cudaEvent_t ev : events) cudaEventDestroy(ev);
-    return result != KLEIDICV_OK ? result : se;
-  };
-  if ((s.dev_bytes && !s.dev) || (d.dev_bytes && !d.dev)) return finish(KLEIDICV_ERROR_ALLOCATION);
+  if ((s.dev_bytes && !s.dev) || (d.dev_bytes && !d.dev)) return KLEIDICV_ERROR_ALLOCATION;
 
   // Upload phase: the scheduler runs the source stripes.
+  kleidicv_error_t e;
   if (!s.on_device) {
     Transfer x{ctx, &s, nullptr};
     e = mt.parallel(upload_task, &x, mt.parallel_data, s.tasks);
-    if (e != KLEIDICV_OK) return finish(e);
+    if (e != KLEIDICV_OK) return e;
   }
   e = op(s.dev, s.pitch, d.dev, d.pitch, ctx);
-  if (e != KLEIDICV_OK) return finish(e);
-  if (d.on_device) return finish(KLEIDICV_OK);
-  // Download phase: one copy and one event per destination stripe, then the
-  // scheduler unpacks stripes as their copies land.
-  events.resize(d.tasks, nullptr);
-  for (unsigned t = 0; t < d.tasks; ++t) {
-    const size_t r0 = static_cast<size_t>(t) * d.rows_per_task;
-    const size_t r1 = std::min(d.img.rows, r0 + d.rows_per_task);
-    cudaError_t ce = cudaEventCreateWithFlags(&events[t], cudaEventDisableTiming);
-    if (ce == cudaSuccess) {
-      if (d.pinned)
-        ce = cudaMemcpy2DAsync(const_cast<uint8_t *>(d.img.ptr) + r0 * d.img.stride, d.img.stride,
-                               d.dev + r0 * d.pitch, d.pitch, d.img.row_bytes, r1 - r0,
+  if (e != KLEIDICV_OK) return e;
+  if (!d.on_device) {
+    events.resize(d.tasks, nullptr);
+    for (unsigned t = 0; t < d.tasks; ++t) {
+      const size_t r0 = static_cast<size_t>(t) * d.rows_per_task;
+      const size_t r1 = std::min(d.img.rows, r0 + d.rows_per_task);
+      cudaError_t ce = cudaEventCreateWithFlags(&events[t], cudaEventDisableTiming);
+      if (ce == cudaSuccess) {
+        if (d.pinned)
+          ce = cudaMemcpy2DAsync(const_cast<uint8_t *>(d.img.ptr) + r0 * d.img.stride, d.img.stride,
+                                 d.dev + r0 * d.pitch, d.pitch, d.img.row_bytes, r1 - r0,
+                                 cudaMemcpyDeviceToHost, ctx->stream);
+        else
+          ce = cudaMemcpyAsync(d.stage + r0 * d.pitch, d.dev + r0 * d.pitch, (r1 - r0) * d.pitch,
                                cudaMemcpyDeviceToHost, ctx->stream);
-      else
-        ce = cudaMemcpyAsync(d.stage + r0 * d.pitch, d.dev + r0 * d.pitch, (r1 - r0) * d.pitch,
-                             cudaMemcpyDeviceToHost, ctx->stream);
-    }
-    if (ce == cudaSuccess) ce = cudaEventRecord(events[t], ctx->stream);
-    if (ce != cudaSuccess) {
-      events.resize(t + (events[t] ? 1 : 0));
-      return finish(cuda_fail(ctx, ce));
+      }
+      if (ce == cudaSuccess) ce = cudaEventRecord(events[t], ctx->stream);
+      if (ce != cudaSuccess) {
+        events.resize(t + (events[t] ? 1 : 0));
+        return cuda_fail(ctx, ce);
+      }
     }
   }
-  if (!d.pinned) {
+  if (async) {
+    cudaError_t ce = cudaEventCreateWithFlags(&done_event, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventRecord(done_event, ctx->stream);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce);
+  }
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t ThreadedCall::complete(kleidicv_error_t result) {
+  kcv::DeviceGuard guard(ctx->device);
+  // Download phase: the scheduler unpacks stripes as their copies land.
+  if (result == KLEIDICV_OK && !d.on_device && !d.pinned && !events.empty()) {
     Transfer x{ctx, &d, &events};
-    e = mt.parallel(download_task, &x, mt.parallel_data, d.tasks);
-    if (e != KLEIDICV_OK) return finish(e);
+    result = mt.parallel(download_task, &x, mt.parallel_data, d.tasks);
   }
-  return finish(KLEIDICV_OK);
+  if (!s.on_device) kcv::ctx_free(ctx, s.dev, s.dev_bytes);
+  if (!d.on_device) kcv::ctx_free(ctx, d.dev, d.dev_bytes);
+  kleidicv_error_t se;
+  if (async) {
+    // Only this call's work: later calls on the stream need not have finished.
+    const cudaError_t ce = done_event ? cudaEventSynchronize(done_event) : cudaSuccess;
+    se = ce == cudaSuccess ? KLEIDICV_OK : cuda_fail(ctx, ce);
+    if (done_event) cudaEventDestroy(done_event);
+    done_event = nullptr;
+    pool_return(ctx, staging, staging_bytes);
+    staging = nullptr;
+  } else {
+    se = kleidicv_gpu_context_synchronize(ctx);
+  }
+  for (cudaEvent_t ev : events) cudaEventDestroy(ev);
+  events.clear();
+  return result != KLEIDICV_OK ? result : se;
+}
+
+kleidicv_error_t run_threaded(kleidicv_error_t validation, const Prepared &p, HostImage src,
+                              HostImage dst, const DeviceOp &op,
+                              kleidicv_thread_multithreading mt) {
+  if (validation != KLEIDICV_OK) return validation;
+  if (!mt.parallel) return KLEIDICV_ERROR_NULL_POINTER;
+  if (p.kind == Prepared::NOTHING) return KLEIDICV_OK;
+  ThreadedCall call;
+  kleidicv_error_t e = kcv::resolve_context(call.ctx);
+  if (e != KLEIDICV_OK) return e;
+  call.mt = mt;
+  e = call.begin(p, src, dst, op);
+  return call.complete(e);
+}
+
+}  // namespace
+
+// An asynchronous threaded call in flight (include/kleidicv_gpu_thread.h).
+struct kleidicv_gpu_async {
+  ThreadedCall call;
+  kleidicv_gpu_async_callback done = nullptr;
+  void *user_data = nullptr;
+  bool caller_owns = false;
+  mutable std::mutex m;
+  std::condition_variable cv;
+  bool complete = false;
+  kleidicv_error_t status = KLEIDICV_OK;
+};
+
+namespace {
+
+// Completion worker of a context: finishes queued asynchronous calls in
+// submission order (they share the context's stream, so they also complete
+// in that order).
+void async_worker_loop(kleidicv_gpu_context_t *ctx) {
+  for (;;) {
+    kleidicv_gpu_async *a = nullptr;
+    {
+      std::unique_lock<std::mutex> l(ctx->async_mutex);
+      ctx->async_cv.wait(l, [&] { return ctx->async_stop || !ctx->async_queue.empty(); });
+      if (ctx->async_queue.empty()) return;  // stopping, nothing left
+      a = ctx->async_queue.front();
+      ctx->async_queue.pop_front();
+    }
+    const kleidicv_error_t st = a->call.complete(KLEIDICV_OK);
+    if (a->done) a->done(st, a->user_data);
+    if (!a->caller_owns) {
+      delete a;
+      continue;
+    }
+    // The caller may free the handle as soon as it sees `complete`: notify
+    // under the lock and touch nothing afterwards.
+    std::lock_guard<std::mutex> l(a->m);
+    a->status = st;
+    a->complete = true;
+    a->cv.notify_all();
+  }
+}
+
+kleidicv_error_t run_threaded_async(kleidicv_error_t validation, const Prepared &p, HostImage src,
+                                    HostImage dst, const DeviceOp &op,
+                                    kleidicv_thread_multithreading mt,
+                                    kleidicv_gpu_async_callback done, void *user_data,
+                                    kleidicv_gpu_async_t **handle) {
+  if (handle) *handle = nullptr;
+  if (validation != KLEIDICV_OK) return validation;
+  if (!mt.parallel) return KLEIDICV_ERROR_NULL_POINTER;
+  kleidicv_gpu_context_t *ctx = nullptr;
+  kleidicv_error_t e = kcv::resolve_context(ctx);
+  if (e != KLEIDICV_OK) return e;
+  auto *a = new kleidicv_gpu_async();
+  a->call.ctx = ctx;
+  a->call.mt = mt;
+  a->call.async = true;
+  a->done = done;
+  a->user_data = user_data;
+  a->caller_owns = handle != nullptr;
+  if (p.kind != Prepared::NOTHING) {
+    e = a->call.begin(p, src, dst, op);
+    if (e != KLEIDICV_OK) {
+      a->call.complete(e);  // releases what begin() took
+      delete a;
+      return e;
+    }
+  }
+  {
+    std::lock_guard<std::mutex> l(ctx->async_mutex);
+    if (!ctx->async_worker.joinable()) ctx->async_worker = std::thread(async_worker_loop, ctx);
+    ctx->async_queue.push_back(a);
+  }
+  ctx->async_cv.notify_one();
+  if (handle) *handle = a;
+  return KLEIDICV_OK;
 }
 
 }  // namespace
@@ -481,3 +644,136 @@ kleidicv_error_t kleidicv_gpu_thread_sobel_3x3_vertical_s16_u8(
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Asynchronous variants: the same validation and device work, finished by the
+// context's completion worker.
+extern "C" {
+
+kleidicv_error_t kleidicv_gpu_thread_gaussian_blur_u8_async(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, size_t kernel_width, size_t kernel_height, float sigma_x,
+    float sigma_y, kleidicv_border_type_t border_type, kleidicv_thread_multithreading mt,
+    kleidicv_gpu_async_callback done, void *user_data, kleidicv_gpu_async_t **handle) {
+  Prepared p;
+  const kleidicv_error_t v =
+      kcv::prepare_gaussian(src, src_stride, dst, dst_stride, width, height, channels,
+                            kernel_width, kernel_height, sigma_x, sigma_y, border_type, false, 0,
+                            &p);
+  const size_t rb = width * channels;
+  return run_threaded_async(
+      v, p, {src, src_stride, rb, height}, {dst, dst_stride, rb, height},
+      [=](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_gaussian_blur_u8(static_cast<const uint8_t *>(s), ss,
+                                             static_cast<uint8_t *>(d), ds, width, height, channels,
+                                             kernel_width, kernel_height, sigma_x, sigma_y,
+                                             border_type, c);
+      },
+      mt, done, user_data, handle);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u8_async(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint8_t *kernel_x, size_t kernel_width,
+    const uint8_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_separable(1, src, src_stride, dst, dst_stride, width,
+                                                    height, channels, kernel_x, kernel_width,
+                                                    kernel_y, kernel_height, border_type, false,
+                                                    0, &p);
+  const size_t rb = width * channels;
+  return run_threaded_async(
+      v, p, {src, src_stride, rb, height}, {dst, dst_stride, rb, height},
+      [=](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_separable_filter_2d_u8(static_cast<const uint8_t *>(s), ss,
+                                                   static_cast<uint8_t *>(d), ds, width, height,
+                                                   channels, kernel_x, kernel_width, kernel_y,
+                                                   kernel_height, border_type, c);
+      },
+      mt, done, user_data, handle);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_separable_filter_2d_u16_async(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride, size_t width,
+    size_t height, size_t channels, const uint16_t *kernel_x, size_t kernel_width,
+    const uint16_t *kernel_y, size_t kernel_height, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_separable(2, src, src_stride, dst, dst_stride, width,
+                                                    height, channels, kernel_x, kernel_width,
+                                                    kernel_y, kernel_height, border_type, false,
+                                                    0, &p);
+  const size_t rb = width * channels * 2;
+  return run_threaded_async(
+      v, p, {reinterpret_cast<const uint8_t *>(src), src_stride, rb, height},
+      {reinterpret_cast<const uint8_t *>(dst), dst_stride, rb, height},
+      [=](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_separable_filter_2d_u16(static_cast<const uint16_t *>(s), ss,
+                                                    static_cast<uint16_t *>(d), ds, width, height,
+                                                    channels, kernel_x, kernel_width, kernel_y,
+                                                    kernel_height, border_type, c);
+      },
+      mt, done, user_data, handle);
+}
+
+kleidicv_error_t kleidicv_gpu_thread_blur_and_downsample_u8_async(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height, uint8_t *dst,
+    size_t dst_stride, size_t channels, kleidicv_border_type_t border_type,
+    kleidicv_thread_multithreading mt, kleidicv_gpu_async_callback done, void *user_data,
+    kleidicv_gpu_async_t **handle) {
+  Prepared p;
+  const kleidicv_error_t v = kcv::prepare_blurdown(src, src_stride, src_width, src_height, dst,
+                                                   dst_stride, channels, border_type, false, 0, &p);
+  return run_threaded_async(
+      v, p, {src, src_stride, src_width * channels, src_height},
+      {dst, dst_stride, (src_width + 1) / 2 * channels, (src_height + 1) / 2},
+      [=](const void *s, size_t ss, void *d, size_t ds, kleidicv_gpu_context_t *c) {
+        return kleidicv_gpu_blur_and_downsample_u8(static_cast<const uint8_t *>(s), ss, src_width,
+                                                   src_height, static_cast<uint8_t *>(d), ds,
+                                                   channels, border_type, c);
+      },
+      mt, done, user_data, handle);
+}
+
+kleidicv_error_t kleidicv_gpu_async_query(const kleidicv_gpu_async_t *handle) {
+  if (!handle) return KLEIDICV_ERROR_NULL_POINTER;
+  std::lock_guard<std::mutex> l(handle->m);
+  return handle->complete ? handle->status : KLEIDICV_GPU_ERROR_NOT_READY;
+}
+
+kleidicv_error_t kleidicv_gpu_async_wait(kleidicv_gpu_async_t *handle) {
+  if (!handle) return KLEIDICV_ERROR_NULL_POINTER;
+  std::unique_lock<std::mutex> l(handle->m);
+  handle->cv.wait(l, [&] { return handle->complete; });
+  return handle->status;
+}
+
+kleidicv_error_t kleidicv_gpu_async_release(kleidicv_gpu_async_t *handle) {
+  if (!handle) return KLEIDICV_ERROR_NULL_POINTER;
+  kleidicv_gpu_async_wait(handle);
+  delete handle;
+  return KLEIDICV_OK;
+}
+
+}  // extern "C"
+
+namespace kcv {
+
+// Joins the context's completion worker after it has finished every queued
+// call, and frees the pooled staging (kleidicv_gpu_context_destroy).
+void shutdown_async(kleidicv_gpu_context_t *ctx) {
+  {
+    std::lock_guard<std::mutex> l(ctx->async_mutex);
+    ctx->async_stop = true;
+  }
+  ctx->async_cv.notify_all();
+  if (ctx->async_worker.joinable()) ctx->async_worker.join();
+  std::lock_guard<std::mutex> l(ctx->pinned_pool_mutex);
+  for (auto &b : ctx->pinned_pool) cudaFreeHost(b.first);
+  ctx->pinned_pool.clear();
+}
+
+}  // namespace kcv
