@@ -72,6 +72,10 @@ def parse_args():
                     help="run one workload 3 times on cuda:0 and exit (a small command for profiler captures): "
                          "the sweep's Gaussian / u16 REFLECT / s16 REFLECT call, blur_and_downsample_u8 of a "
                          "4096x4096x1 image, or the d/dx Sobel of a 3840x2160x1 image")
+    ap.add_argument("--profile-range", type=int, default=0,
+                    help="with --profile-op: N calls over rotating buffer sets larger than twice the L2, between "
+                         "cudaProfilerStart and cudaProfilerStop (an ncu --replay-mode range window that also "
+                         "holds the write-back of earlier calls' outputs)")
     ap.add_argument("--serving-seconds", type=float, default=60.0)
     ap.add_argument("--serving-high-seconds", type=float, default=10.0)
     ap.add_argument("--serving-inflight", type=int, default=3)
@@ -841,56 +845,82 @@ def _pyr_image(rng, w, h, c):
 
 def section_pyramid(torch, kcv, ctx, stream):
     """Seed 3: 8192x8192x1 and 4096x4096x3 through 5 blur_and_downsample
-    levels (REVERSE), and 64 pyramids of 1024x768x4 as batched plans."""
+    levels (REVERSE), each pyramid one launch; and 64 pyramids of 1024x768x4,
+    5 levels each, in one launch.  Source and level buffers rotate over sets
+    whose total exceeds twice the L2, so every call reads its level 0 from
+    HBM.  Every level of the first set is compared with the CPU oracle."""
     from oracle import oracle
 
     rng = np.random.default_rng(3)
+    l2 = 2 * 129 * 1024 * 1024
     out = {}
+
+    def levels_of(w, h):
+        sizes = []
+        for _ in range(5):
+            w, h = (w + 1) // 2, (h + 1) // 2
+            sizes.append((w, h))
+        return sizes
+
+    def check(host, w, h, c, dsts):
+        level, lw, lh = host, w, h
+        for d in dsts:
+            e, level = oracle.blur_and_downsample_u8(level, lw, lh, c, kcv.REVERSE, nthreads=os.cpu_count() or 1)
+            lw, lh = (lw + 1) // 2, (lh + 1) // 2
+            if e != 0 or not np.array_equal(d.cpu().numpy(), level):
+                return False
+        return True
+
     for (w, h, c) in ((8192, 8192, 1), (4096, 4096, 3)):
         host = _pyr_image(rng, w, h, c)
-        src = torch.from_numpy(host).cuda()
-        sizes, ww, hh = [], w, h
-        for _ in range(5):
-            ww, hh = (ww + 1) // 2, (hh + 1) // 2
-            sizes.append((ww, hh))
-        dsts = [torch.empty((hh_, ww_ * c), dtype=torch.uint8, device="cuda") for ww_, hh_ in sizes]
+        sizes = levels_of(w, h)
+        per_set = host.nbytes + sum(ww * hh * c for ww, hh in sizes)
+        nsets = max(2, -(-l2 // per_set) + 1)
+        sets = []
+        for _ in range(nsets):
+            src = torch.from_numpy(host).cuda()
+            sets.append((src, [torch.empty((hh_, ww_ * c), dtype=torch.uint8, device="cuda") for ww_, hh_ in sizes]))
 
-        def run(i):
+        def run(i, sets=sets, w=w, h=h, c=c):
+            src, dsts = sets[i % len(sets)]
             e = kcv.build_pyramid_u8(src.data_ptr(), w * c, w, h, c, [d.data_ptr() for d in dsts],
                                      [d.stride(0) for d in dsts], kcv.REVERSE, ctx)
             assert e == kcv.OK
 
-        run(0)
-        ms = _events_time(torch, stream, run, 10)
-        _, l1 = oracle.blur_and_downsample_u8(host, w, h, c, kcv.REVERSE)
-        nbytes = host.nbytes + sum(d.numel() for d in dsts)
-        out[f"{w}x{h}x{c}"] = {"ms": round(ms, 3), "mpix_s_level0": round(w * h / (ms * 1e-3) / 1e6, 1),
-                               "hbm_gbs": round(nbytes / (ms * 1e-3) / 1e9, 1),
-                               "level1_bit_exact": bool(np.array_equal(dsts[0].cpu().numpy(), l1))}
-    # 64 pyramids of 1024x768x4: one batch plan per level, replayed as graphs.
+        for i in range(3):
+            run(i)
+        ms = _events_time(torch, stream, run, 20)
+        torch.cuda.synchronize()
+        out[f"{w}x{h}x{c}"] = {"ms": round(ms, 4), "mpix_s_level0": round(w * h / (ms * 1e-3) / 1e6, 1),
+                               "hbm_gbs": round(per_set / (ms * 1e-3) / 1e9, 1), "launches_per_pyramid": 1,
+                               "rotating_sets": nsets, "all_levels_bit_exact": check(host, w, h, c, sets[0][1])}
+        del sets
+    # 64 pyramids of 1024x768x4, 5 levels each: one launch.
     w, h, c = 1024, 768, 4
-    srcs = [torch.from_numpy(_pyr_image(rng, w, h, c)).cuda() for _ in range(64)]
-    levels, prev, pw, ph = [], srcs, w, h
-    plans = []
-    for _ in range(5):
-        nw, nh = (pw + 1) // 2, (ph + 1) // 2
-        outs = [torch.empty((nh, nw * c), dtype=torch.uint8, device="cuda") for _ in range(64)]
-        reqs = [kcv.make_request(kcv.OP_BLUR_AND_DOWNSAMPLE_U8, a.data_ptr(), pw * c, b.data_ptr(), nw * c, pw,
-                                 ph, c, border_type=kcv.REVERSE) for a, b in zip(prev, outs)]
-        plans.append(kcv.BatchPlan(reqs, ctx))
-        levels.append(outs)
-        prev, pw, ph = outs, nw, nh
+    sizes = levels_of(w, h)
+    hosts = [_pyr_image(rng, w, h, c) for _ in range(64)]
+    per_set = 64 * (w * h * c + sum(ww * hh * c for ww, hh in sizes))
+    nsets = max(2, -(-l2 // per_set) + 1)
+    bsets = []
+    for _ in range(nsets):
+        srcs = [torch.from_numpy(hh).cuda() for hh in hosts]
+        dsts = [[torch.empty((lh, lw * c), dtype=torch.uint8, device="cuda") for lw, lh in sizes] for _ in srcs]
+        bsets.append((srcs, dsts))
 
     def run_b(i):
-        for p in plans:
-            assert p.launch(True) == kcv.OK
+        srcs, dsts = bsets[i % len(bsets)]
+        err, _ = kcv.build_pyramids_u8([(s_.data_ptr(), w * c, w, h, c, [d.data_ptr() for d in ds],
+                                         [d.stride(0) for d in ds], kcv.REVERSE) for s_, ds in zip(srcs, dsts)], ctx)
+        assert err == kcv.OK
 
-    run_b(0)
-    ms = _events_time(torch, stream, run_b, 10)
-    out["batched_64x1024x768x4"] = {"ms": round(ms, 3),
-                                    "mpix_s_level0": round(64 * w * h / (ms * 1e-3) / 1e6, 1)}
-    for p in plans:
-        p.close()
+    for i in range(3):
+        run_b(i)
+    ms = _events_time(torch, stream, run_b, 20)
+    torch.cuda.synchronize()
+    exact = all(check(hosts[k], w, h, c, bsets[0][1][k]) for k in (0, 31, 63))
+    out["batched_64x1024x768x4"] = {"ms": round(ms, 4), "mpix_s_level0": round(64 * w * h / (ms * 1e-3) / 1e6, 1),
+                                    "hbm_gbs": round(per_set / (ms * 1e-3) / 1e9, 1), "launches": 1,
+                                    "rotating_sets": nsets, "all_levels_bit_exact_sample": exact}
     return out
 
 
@@ -1229,8 +1259,10 @@ def reference_arm(args, calls, config):
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def profile_op(name):
-    """One workload, three calls, for a profiler capture (`--profile-op`)."""
+def profile_op(name, range_calls=0):
+    """One workload for a profiler capture (`--profile-op`): three calls, or
+    with range_calls > 0 one call, then range_calls calls over rotating buffer
+    sets (more than twice the L2 in total) inside a profiler range."""
     import torch
     import __graft_entry__ as ge
 
@@ -1240,37 +1272,55 @@ def profile_op(name):
     rng = np.random.default_rng(3)
     if name in ("gauss", "u16", "s16"):
         c = {"gauss": calls[0], "u16": calls[1], "s16": calls[4]}[name]
-        src = torch.from_numpy(c["src"].view(np.uint8)).cuda()
-        dst = torch.empty_like(src)
+        host = c["src"].view(np.uint8)
+        out_shape, out_dtype = host.shape, torch.uint8
+    elif name == "blurdown":
+        host = _pyr_image(rng, 4096, 4096, 1)
+        out_shape, out_dtype = (2048, 2048), torch.uint8
+    else:
+        host = rng.integers(0, 256, (H, W), dtype=np.uint8)
+        out_shape, out_dtype = (H, W), torch.int16
+    nbytes = 2 * host.nbytes
+    nsets = max(1, -(-2 * 129 * 1024 * 1024 // nbytes) + 1) if range_calls else 1
+    sets = [(torch.from_numpy(host).cuda(), torch.empty(out_shape, dtype=out_dtype, device="cuda"))
+            for _ in range(nsets)]
+
+    def f(i):
+        src, dst = sets[i % nsets]
         ss = src.stride(0)
         if name == "gauss":
-            f = lambda: kcv.gaussian_blur_u8(src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 4, 7, 7, 1.5, 1.5,  # noqa
-                                             c["border"], ctx)
-        else:
-            f = lambda: kcv.separable_filter_2d(c["dtype"], src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 1,  # noqa
-                                                c["kx"], 5, c["ky"], 5, c["border"], ctx, border_value=c["bv"])
-    elif name == "blurdown":
-        src = torch.from_numpy(_pyr_image(rng, 4096, 4096, 1)).cuda()
-        dst = torch.empty((2048, 2048), dtype=torch.uint8, device="cuda")
-        f = lambda: kcv.blur_and_downsample_u8(src.data_ptr(), 4096, 4096, 4096, dst.data_ptr(), 2048, 1,  # noqa
-                                               kcv.REVERSE, ctx)
-    else:
-        src = torch.from_numpy(rng.integers(0, 256, (H, W), dtype=np.uint8)).cuda()
-        dst = torch.empty((H, W), dtype=torch.int16, device="cuda")
-        f = lambda: kcv.sobel_3x3_horizontal_s16_u8(src.data_ptr(), W, dst.data_ptr(), 2 * W, W, H, 1, ctx)  # noqa
-    for _ in range(3):
-        if f() != kcv.OK:
+            return kcv.gaussian_blur_u8(src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 4, 7, 7, 1.5, 1.5,
+                                        c["border"], ctx)
+        if name in ("u16", "s16"):
+            return kcv.separable_filter_2d(c["dtype"], src.data_ptr(), ss, dst.data_ptr(), ss, W, H, 1, c["kx"], 5,
+                                           c["ky"], 5, c["border"], ctx, border_value=c["bv"])
+        if name == "blurdown":
+            return kcv.blur_and_downsample_u8(src.data_ptr(), 4096, 4096, 4096, dst.data_ptr(), 2048, 1,
+                                              kcv.REVERSE, ctx)
+        return kcv.sobel_3x3_horizontal_s16_u8(src.data_ptr(), W, dst.data_ptr(), 2 * W, W, H, 1, ctx)
+
+    n = 3 if not range_calls else 1
+    for i in range(n):
+        if f(i) != kcv.OK:
             raise RuntimeError(f"{name} call failed")
+    if range_calls:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        for i in range(range_calls):
+            if f(1 + i) != kcv.OK:
+                raise RuntimeError(f"{name} call failed")
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     if ctx.synchronize() != kcv.OK:
         raise RuntimeError(f"{name} failed on the device")
     ctx.close()
-    print(f"profile-op {name}: 3 calls done", flush=True)
+    print(f"profile-op {name}: done ({n} + {range_calls} calls, {nsets} buffer sets)", flush=True)
 
 
 def main():
     args = parse_args()
     if args.profile_op:
-        profile_op(args.profile_op)
+        profile_op(args.profile_op, args.profile_range)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

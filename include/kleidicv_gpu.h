@@ -340,6 +340,23 @@ kleidicv_error_t kleidicv_gpu_batch_submit(const kleidicv_gpu_request_t *request
                                            kleidicv_error_t *statuses,
                                            kleidicv_gpu_context_t *ctx);
 
+/* Many image pyramids in one launch per channel count (no reference
+ * counterpart: the reference builds every pyramid level by level).  Each
+ * entry is validated like kleidicv_gpu_build_pyramid_u8 (statuses[i] is its
+ * result, statuses may be NULL); valid entries are computed, level l of every
+ * image before level l + 1 of any.  Returns the first failing entry's status
+ * (nothing is launched then) or a CUDA failure. */
+typedef struct {
+  const uint8_t *src;
+  size_t src_stride, src_width, src_height, channels, levels;
+  uint8_t *const *dst;
+  const size_t *dst_strides;
+  kleidicv_border_type_t border_type;
+} kleidicv_gpu_pyramid_t;
+kleidicv_error_t kleidicv_gpu_build_pyramids_u8(const kleidicv_gpu_pyramid_t *pyramids,
+                                                size_t count, kleidicv_error_t *statuses,
+                                                kleidicv_gpu_context_t *ctx);
+
 /* ------------------------------------------------------------------------ */
 /* Serving loop: requests arrive asynchronously, images stay resident in a
  * capped device pool, requests are admitted by free bytes and by free

@@ -153,3 +153,38 @@ def test_batch_of_nothing_and_only_rejects():
     plan.close()
     plan2.close()
     ctx.close()
+
+
+def test_uneven_batch_512_all_outputs():
+    """The 512-image uneven batch (seed 2: w 64-4096 and h 64-2160 log-uniform,
+    C {1,3,4}, k {3,5,7,15}, sigma 0.5-4, random border), one graph launch of
+    one plan: every output equals the oracle's."""
+    rng = np.random.default_rng(2)
+    ctx = kcv.Context.for_torch(0)
+    items = []
+    for _ in range(512):
+        w = int(round(float(np.exp(rng.uniform(np.log(64), np.log(4096))))))
+        h = int(round(float(np.exp(rng.uniform(np.log(64), np.log(2160))))))
+        c = int(rng.choice([1, 3, 4]))
+        k = int(rng.choice([3, 5, 7, 15]))
+        sigma = float(rng.uniform(0.5, 4.0))
+        border = int(rng.choice([kcv.REPLICATE, kcv.REFLECT, kcv.WRAP, kcv.REVERSE]))
+        host = rng.integers(0, 256, (h, w * c), dtype=np.uint8)
+        src = torch.from_numpy(host).cuda()
+        dst = torch.zeros_like(src)
+        items.append((host, src, dst, w, h, c, k, sigma, border))
+    reqs = [kcv.make_request(kcv.OP_GAUSSIAN_BLUR_U8, it[1].data_ptr(), it[3] * it[5], it[2].data_ptr(),
+                             it[3] * it[5], it[3], it[4], it[5], it[6], it[6], it[7], it[7], border_type=it[8])
+            for it in items]
+    plan = kcv.BatchPlan(reqs, ctx)
+    assert all(st == kcv.OK for st in plan.statuses)
+    assert plan.launch(True) == kcv.OK
+    assert ctx.synchronize() == kcv.OK
+    bad = []
+    for i, it in enumerate(items):
+        e, want = oracle.gaussian_blur_u8(it[0], it[3], it[4], it[5], it[6], it[7], it[8], nthreads=16)
+        if e != 0 or not np.array_equal(it[2].cpu().numpy(), want):
+            bad.append(i)
+    plan.close()
+    ctx.close()
+    assert not bad, f"{len(bad)} of 512 outputs differ, first {bad[:5]}"

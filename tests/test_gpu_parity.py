@@ -120,10 +120,10 @@ def test_gaussian_misaligned_and_padded(kcv, oracle, ctx, offset):
 SEP_DT = {"u8": np.uint8, "u16": np.uint16, "s16": np.int16}
 
 
-def run_separable(kcv, ctx, dt, host, w, h, c, kx, ky, border, bv=None, offset=0):
+def run_separable(kcv, ctx, dt, host, w, h, c, kx, ky, border, bv=None, offset=0, dst_pad=3):
     dtype = SEP_DT[dt]
     _keep, sp, ss = device_image(torch, host, offset)
-    obuf, dp, ds = device_output(torch, h, w * c, dtype, 3)
+    obuf, dp, ds = device_output(torch, h, w * c, dtype, dst_pad)
     err = kcv.separable_filter_2d(dt, sp, ss, dp, ds, w, h, c, kx, 5, ky, 5, border, ctx, border_value=bv)
     assert err == kcv.OK, kcv.ERROR_NAMES.get(err, err)
     assert ctx.synchronize() == kcv.OK
@@ -150,6 +150,44 @@ def test_separable(kcv, oracle, ctx, dt, c):
                 assert err == oracle.OK
                 assert pad_ok
                 assert np.array_equal(got, want), (dt, c, border, w, h, trange)
+
+
+@pytest.mark.parametrize("dt", ["u16", "s16"])
+def test_separable_16bit_5x5_one_channel(kcv, oracle, ctx, dt):
+    """The one-channel 16-bit 5x5 streaming kernel: several warp strips and
+    bands (heights not a multiple of its 5-row step), ragged widths, a source
+    8 bytes off 16-byte alignment (element gathers), every border, full-range
+    taps (u16 saturation), and s16 taps exactly at and just past the limit of
+    its fp32 path (32768 * sum|kx| * sum|ky| <= 2^24; past it the generic
+    kernel runs)."""
+    dtype = SEP_DT[dt]
+    info = np.iinfo(dtype)
+    rng = np.random.default_rng(91 + len(dt))
+    sizes = [(241, 37), (480, 11), (723, 203), (1999, 64), (16, 7), (9, 5)]
+    borders = BORDERS + [0]
+    taps = [(rng.integers(0, 5, 5), rng.integers(0, 5, 5))] if dt == "u16" else \
+        [(rng.integers(-4, 5, 5), rng.integers(-4, 5, 5))]
+    if dt == "u16":
+        taps.append((rng.integers(0, 65536, 5), rng.integers(0, 65536, 5)))
+        taps.append((np.array([0, 0, 65535, 0, 0]), np.array([1, 0, 0, 0, 0])))
+    else:
+        taps.append((np.array([-8, 4, 0, 2, 2]), np.array([1, -9, 0, 4, 2])))   # 16 * 16 * 32768 = 2^23
+        taps.append((np.array([-16, 8, 0, 4, 4]), np.array([1, -9, 0, 4, 2])))  # 32 * 16 = 512: at the limit
+        taps.append((np.array([-16, 8, 0, 4, 5]), np.array([1, -9, 0, 4, 2])))  # 33 * 16: generic kernel
+        taps.append((rng.integers(-32768, 32768, 5), rng.integers(-32768, 32768, 5)))
+    for i, (w, h) in enumerate(sizes):
+        for border in borders:
+            kx, ky = taps[(i + border) % len(taps)]
+            offset = 8 if (i + border) % 3 == 0 else 0
+            pad = (8 - w % 8) % 8 + 8  # rows a multiple of 16 bytes
+            host = padded(rng, h, w, dtype, pad, low=int(info.min), high=int(info.max))
+            bv = 4097 if border == 0 else None
+            got, pad_ok = run_separable(kcv, ctx, dt, host, w, h, 1, kx, ky, border, bv, offset=offset,
+                                        dst_pad=pad if border % 2 else 3)
+            err, want = oracle.separable_filter_2d(host, w, h, 1, kx.astype(dtype), ky.astype(dtype), border,
+                                                   ext=bv is not None, border_value=bv or 0)
+            assert err == oracle.OK and pad_ok
+            assert np.array_equal(got, want), (dt, w, h, border, offset, kx.tolist(), ky.tolist())
 
 
 @pytest.mark.parametrize("dt", ["u8", "u16"])
@@ -286,3 +324,85 @@ def test_arbitrary_size_right_border_lanes(kcv, oracle, ctx, k, w, c):
     rng = np.random.default_rng(k * 10 + c)
     for sigma in (0.0, 3.0):
         check_gaussian(kcv, oracle, ctx, rng, w, k + 3, c, k, sigma, 1)
+
+
+def _pyramid_levels(oracle, host, w, h, c, levels, border):
+    out, level, lw, lh = [], host, w, h
+    for _ in range(levels):
+        e, level = oracle.blur_and_downsample_u8(level, lw, lh, c, border)
+        assert e == 0
+        lw, lh = (lw + 1) // 2, (lh + 1) // 2
+        out.append(level)
+    return out
+
+
+@pytest.mark.parametrize("c", [1, 2, 3, 4])
+def test_pyramid_one_launch_many_levels(kcv, oracle, ctx, c):
+    """Pyramids built in one cooperative launch (more levels than one launch
+    carries inline, so also two launches), ragged sizes, every border."""
+    rng = np.random.default_rng(40 + c)
+    for (w, h, levels, border) in [(2001, 1499, 9, 4), (1030, 777, 7, 1), (133, 67, 4, 2), (4099, 259, 6, 3)]:
+        host = padded(rng, h, w * c, np.uint8, 0)
+        _k, sp, ss = device_image(torch, host)
+        sizes = pyr_sizes(w, h, levels)
+        outs = [device_output(torch, lh, lw * c, np.uint8, 3) for (lw, lh) in sizes]
+        err = kcv.build_pyramid_u8(sp, ss, w, h, c, [o[1] for o in outs], [o[2] for o in outs], border, ctx)
+        assert err == kcv.OK
+        assert ctx.synchronize() == kcv.OK
+        for lv, ((ow, oh), (buf, _p, st), want) in enumerate(zip(sizes, outs, _pyramid_levels(
+                oracle, host, w, h, c, levels, border))):
+            got, pad_ok = read_output(buf, oh, ow * c, np.uint8, st)
+            assert pad_ok, (c, w, h, lv)
+            assert np.array_equal(got, want), (c, w, h, border, lv)
+
+
+def test_pyramids_batched_one_launch(kcv, oracle, ctx):
+    """Many pyramids of mixed channel counts, sizes, borders and level counts
+    through kleidicv_gpu_build_pyramids_u8, plus a misaligned source (byte
+    loads) and an invalid entry reported per entry."""
+    rng = np.random.default_rng(77)
+    cases, keep, expect = [], [], []
+    for i in range(24):
+        c = int(rng.choice([1, 3, 4]))
+        w, h = int(rng.integers(40, 700)), int(rng.integers(40, 500))
+        levels = int(rng.integers(1, 5))
+        border = int(rng.choice([1, 2, 3, 4]))
+        host = padded(rng, h, w * c, np.uint8, 1)
+        buf, sp, ss = device_image(torch, host, offset=1 if i == 5 else 0)
+        sizes = pyr_sizes(w, h, levels)
+        outs = [device_output(torch, lh, lw * c, np.uint8, 0) for (lw, lh) in sizes]
+        keep += [buf, outs]
+        cases.append((sp, ss, w, h, c, [o[1] for o in outs], [o[2] for o in outs], border))
+        expect.append((host, w, h, c, levels, border, sizes, outs))
+    err, st = kcv.build_pyramids_u8(cases, ctx)
+    assert err == kcv.OK and st == [kcv.OK] * len(cases)
+    assert ctx.synchronize() == kcv.OK
+    for host, w, h, c, levels, border, sizes, outs in expect:
+        for (ow, oh), (buf, _p, stv), want in zip(sizes, outs, _pyramid_levels(oracle, host, w, h, c, levels,
+                                                                               border)):
+            got, _ = read_output(buf, oh, ow * c, np.uint8, stv)
+            assert np.array_equal(got, want), (w, h, c, border)
+    bad = list(cases[0])
+    bad[7] = 0  # CONSTANT: not implemented on the drop-in path
+    err, st = kcv.build_pyramids_u8([cases[1], tuple(bad)], ctx)
+    assert err == kcv.NOT_IMPLEMENTED and st == [kcv.OK, kcv.NOT_IMPLEMENTED]
+
+
+def test_blur_and_downsample_tiled_and_pyramid_kernels_agree(kcv, ctx):
+    """A forced tile shape selects the tiled stencil; both kernels give the
+    same bytes."""
+    rng = np.random.default_rng(78)
+    w, h, c = 1001, 707, 3
+    host = padded(rng, h, w * c, np.uint8, 0)
+    _k, sp, ss = device_image(torch, host)
+    ow, oh = (w + 1) // 2, (h + 1) // 2
+    outs = []
+    for tiled in (False, True):
+        if tiled:
+            assert ctx.set_tile_shape(128, 0, 4, 0) == kcv.OK
+        obuf, dp, ds = device_output(torch, oh, ow * c, np.uint8, 0)
+        assert kcv.blur_and_downsample_u8(sp, ss, w, h, dp, ds, c, 2, ctx) == kcv.OK
+        assert ctx.synchronize() == kcv.OK
+        outs.append(read_output(obuf, oh, ow * c, np.uint8, ds)[0])
+    assert ctx.set_tile_shape(0) == kcv.OK
+    assert np.array_equal(outs[0], outs[1])

@@ -49,6 +49,12 @@ class ServerConfig(ctypes.Structure):
                 ("max_queue", _i), ("max_batch_bytes", _sz)]
 
 
+class Pyramid(ctypes.Structure):
+    """kleidicv_gpu_pyramid_t: one image pyramid of a kleidicv_gpu_build_pyramids_u8 call."""
+    _fields_ = [("src", _vp), ("src_stride", _sz), ("src_width", _sz), ("src_height", _sz), ("channels", _sz),
+                ("levels", _sz), ("dst", _vp), ("dst_strides", _vp), ("border_type", _i)]
+
+
 class ThreadMT(ctypes.Structure):
     """kleidicv_thread_multithreading: the caller's scheduler (function pointer) and its data."""
     _fields_ = [("parallel", _vp), ("parallel_data", _vp)]
@@ -127,6 +133,7 @@ SIGNATURES = {
     "kleidicv_gpu_hal_sobel": (_i, [_vp, _sz, _vp, _sz, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i,
                                     ctypes.c_double, ctypes.c_double, _i]),
     "kleidicv_gpu_build_pyramid_u8": (_i, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _i, _vp]),
+    "kleidicv_gpu_build_pyramids_u8": (_i, [ctypes.POINTER(Pyramid), _sz, ctypes.POINTER(_i), _vp]),
     "kleidicv_gpu_batch_plan_create": (_i, [ctypes.POINTER(Request), _sz, ctypes.POINTER(_i),
                                             ctypes.POINTER(_vp), _vp]),
     "kleidicv_gpu_batch_plan_launch": (_i, [_vp, _i, _vp]),
@@ -374,6 +381,22 @@ def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst
     return lib().kleidicv_gpu_build_pyramid_u8(src, src_stride, src_width, src_height, channels, n,
                                                ctypes.cast(dp, ctypes.c_void_p),
                                                ctypes.cast(ds, ctypes.c_void_p), border_type, _h(ctx))
+
+
+def build_pyramids_u8(pyramids, ctx=None):
+    """pyramids: list of (src, src_stride, width, height, channels, dsts, dst_strides, border).
+    Returns (error, statuses)."""
+    n = len(pyramids)
+    arr = (Pyramid * max(n, 1))()
+    keep = []
+    for i, (src, ss, w, h, c, dsts, dss, border) in enumerate(pyramids):
+        dp = (ctypes.c_void_p * max(len(dsts), 1))(*dsts)
+        ds = (ctypes.c_size_t * max(len(dss), 1))(*dss)
+        keep += [dp, ds]
+        arr[i] = Pyramid(src, ss, w, h, c, len(dsts), ctypes.cast(dp, _vp), ctypes.cast(ds, _vp), border)
+    st = (_i * max(n, 1))()
+    err = lib().kleidicv_gpu_build_pyramids_u8(arr, n, st, _h(ctx))
+    return err, list(st)[:n]
 
 
 # --- Lucas-Kanade pyramid ---------------------------------------------------

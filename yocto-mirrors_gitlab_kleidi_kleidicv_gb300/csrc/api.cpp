@@ -484,6 +484,25 @@ kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
                                                 p.row_bytes, p.rows, cudaMemcpyDeviceToDevice,
                                                 ctx->stream));
     case Prepared::FUSED: {
+      if (p.fused.mode == MODE_BLURDOWN && ctx->tune_threads <= 0) {
+        // One level: the tiled blur-and-downsample kernel of pyramid.cu.
+        PyrLaunch L{};
+        pyr_entry(L.inline_entries[0], p.fused.src, p.fused.src_stride, p.fused.dst, p.fused.dst_stride,
+                  p.fused.width, p.fused.height, p.fused.channels, p.fused.border, p.fused.border_value);
+        L.phase_begin[0] = 0;
+        L.phase_begin[1] = 1;
+        L.phases = 1;
+        L.channels = p.fused.channels;
+        L.barrier = reinterpret_cast<unsigned *>(ctx->d_err + 1);
+        L.err_flag = ctx->d_err;
+        ctx->launches += 1;
+        return cuda_status(ctx, launch_pyramid(L, ctx->sm_count, ctx->stream));
+      }
+      if (ctx->tune_threads <= 0 && sep16_eligible(p.fused)) {
+        // One-channel 16-bit 5x5: the fp32 streaming kernel of sep16.cu.
+        ctx->launches += 1;
+        return cuda_status(ctx, launch_sep16(p.fused, ctx->sm_count, ctx->stream));
+      }
       if (ctx->tune_threads > 0) {
         TileShape t{ctx->tune_threads, ctx->tune_tile_rows, ctx->tune_stage_rows, ctx->tune_stages};
         apply_tile_shape(p.fused, t);
@@ -535,8 +554,10 @@ kleidicv_error_t kleidicv_gpu_context_create(kleidicv_gpu_context_t **out, int d
   ctx->stream = static_cast<cudaStream_t>(stream);
   ctx->pool_limit = pool_limit_bytes ? pool_limit_bytes : (40ull << 30);
   ctx->sm_count = prop.multiProcessorCount;
-  if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess ||
-      cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) {
+  // d_err[0]: the device error flag; d_err[1]: the pyramid kernel's grid
+  // barrier counter.
+  if (cudaMalloc(&ctx->d_err, 4 * sizeof(int)) != cudaSuccess ||
+      cudaMemset(ctx->d_err, 0, 4 * sizeof(int)) != cudaSuccess) {
     delete ctx;
     return KLEIDICV_GPU_ERROR_CUDA;
   }
@@ -771,8 +792,109 @@ kleidicv_error_t kleidicv_gpu_build_pyramid_u8(const uint8_t *src, size_t src_st
   kleidicv_error_t e = resolve_context(ctx);
   if (e != KLEIDICV_OK) return e;
   DeviceGuard guard(ctx->device);
-  for (size_t l = 0; l < levels; ++l) {
-    e = execute(ctx, p[l]);
+  if (ctx->tune_threads > 0) {  // a forced tile shape: the tiled stencil, one launch per level
+    for (size_t l = 0; l < levels; ++l) {
+      e = execute(ctx, p[l]);
+      if (e != KLEIDICV_OK) return e;
+    }
+    return KLEIDICV_OK;
+  }
+  // Up to kPyrInline levels per launch, one phase per level.
+  for (size_t l0 = 0; l0 < levels; l0 += kPyrInline) {
+    const size_t n = std::min<size_t>(kPyrInline, levels - l0);
+    PyrLaunch L{};
+    for (size_t k = 0; k < n; ++k) {
+      const FilterJob &j = p[l0 + k].fused;
+      pyr_entry(L.inline_entries[k], j.src, j.src_stride, j.dst, j.dst_stride, j.width, j.height,
+                static_cast<int>(channels), j.border, 0);
+      L.phase_begin[k] = static_cast<int32_t>(k);
+    }
+    L.phase_begin[n] = static_cast<int32_t>(n);
+    L.phases = static_cast<int32_t>(n);
+    L.channels = static_cast<int32_t>(channels);
+    L.barrier = reinterpret_cast<unsigned *>(ctx->d_err + 1);
+    L.err_flag = ctx->d_err;
+    ctx->launches += 1;
+    e = cuda_status(ctx, launch_pyramid(L, ctx->sm_count, ctx->stream));
+    if (e != KLEIDICV_OK) return e;
+  }
+  return KLEIDICV_OK;
+}
+
+kleidicv_error_t kleidicv_gpu_build_pyramids_u8(const kleidicv_gpu_pyramid_t *pyramids, size_t count,
+                                                kleidicv_error_t *statuses, kleidicv_gpu_context_t *ctx) {
+  if (count == 0) return KLEIDICV_OK;
+  if (!pyramids) return KLEIDICV_ERROR_NULL_POINTER;
+  // Validate every level of every pyramid first, as the single call does.
+  std::vector<std::vector<Prepared>> prep(count);
+  kleidicv_error_t first = KLEIDICV_OK;
+  for (size_t i = 0; i < count; ++i) {
+    const kleidicv_gpu_pyramid_t &py = pyramids[i];
+    kleidicv_error_t e = KLEIDICV_OK;
+    if (py.levels > 0 && (!py.dst || !py.dst_strides)) e = KLEIDICV_ERROR_NULL_POINTER;
+    if (py.levels > static_cast<size_t>(kPyrMaxPhases)) e = KLEIDICV_ERROR_RANGE;
+    const uint8_t *s = py.src;
+    size_t ss = py.src_stride, w = py.src_width, h = py.src_height;
+    for (size_t l = 0; e == KLEIDICV_OK && l < py.levels; ++l) {
+      prep[i].emplace_back();
+      e = prepare_blurdown(s, ss, w, h, py.dst[l], py.dst_strides[l], py.channels, py.border_type, false, 0,
+                           &prep[i].back());
+      s = py.dst[l];
+      ss = py.dst_strides[l];
+      w = (w + 1) / 2;
+      h = (h + 1) / 2;
+    }
+    if (statuses) statuses[i] = e;
+    if (e != KLEIDICV_OK && first == KLEIDICV_OK) first = e;
+  }
+  if (first != KLEIDICV_OK) return first;
+  kleidicv_error_t e = resolve_context(ctx);
+  if (e != KLEIDICV_OK) return e;
+  DeviceGuard guard(ctx->device);
+  // One launch per channel count: phase l holds level l + 1 of every image.
+  for (int c = 1; c <= static_cast<int>(kMaxChannels); ++c) {
+    std::vector<PyrEntry> entries;
+    PyrLaunch L{};
+    size_t phases = 0;
+    for (size_t i = 0; i < count; ++i)
+      if (static_cast<int>(pyramids[i].channels) == c) phases = std::max(phases, pyramids[i].levels);
+    if (phases == 0) continue;
+    for (size_t l = 0; l < phases; ++l) {
+      L.phase_begin[l] = static_cast<int32_t>(entries.size());
+      int32_t items = 0;
+      for (size_t i = 0; i < count; ++i) {
+        if (static_cast<int>(pyramids[i].channels) != c || l >= pyramids[i].levels) continue;
+        const FilterJob &j = prep[i][l].fused;
+        PyrEntry en;
+        pyr_entry(en, j.src, j.src_stride, j.dst, j.dst_stride, j.width, j.height, c, j.border, 0);
+        items += en.item_end;
+        en.item_end = items;
+        entries.push_back(en);
+      }
+    }
+    L.phase_begin[phases] = static_cast<int32_t>(entries.size());
+    L.phases = static_cast<int32_t>(phases);
+    L.channels = c;
+    L.barrier = reinterpret_cast<unsigned *>(ctx->d_err + 1);
+    L.err_flag = ctx->d_err;
+    const size_t bytes = entries.size() * sizeof(PyrEntry);
+    PyrEntry *table = nullptr;
+    if (entries.size() <= static_cast<size_t>(kPyrInline)) {
+      std::copy(entries.begin(), entries.end(), L.inline_entries);
+    } else {
+      table = static_cast<PyrEntry *>(ctx_alloc(ctx, bytes));
+      if (!table) return KLEIDICV_ERROR_ALLOCATION;
+      // From pageable memory: the call returns once the table is staged.
+      cudaError_t ce = cudaMemcpyAsync(table, entries.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+      if (ce != cudaSuccess) {
+        ctx_free(ctx, table, bytes);
+        return cuda_status(ctx, ce);
+      }
+      L.entries = table;
+    }
+    ctx->launches += 1;
+    e = cuda_status(ctx, launch_pyramid(L, ctx->sm_count, ctx->stream));
+    if (table) ctx_free(ctx, table, bytes);
     if (e != KLEIDICV_OK) return e;
   }
   return KLEIDICV_OK;

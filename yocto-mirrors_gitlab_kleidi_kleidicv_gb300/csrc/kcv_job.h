@@ -94,6 +94,52 @@ struct FilterJob {
   int32_t box_lbw;          // log2 of the span box width in bytes (8 or 11)
 };
 
+// One-channel 16-bit 5x5 separable filters (csrc/sep16.cu): a warp strip
+// is 32 lanes x 8 elements, of which kSep16Lanes lanes produce output; a
+// warp item is (strip, band of at most kSep16MaxBand destination rows).
+constexpr int kSep16Lanes = 30;
+constexpr int kSep16MaxBand = 15;  // destination rows of a band
+
+struct Sep16Job {
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride, dst_stride;  // bytes
+  int32_t w, h, border, border_value;
+  float kx[5], ky[5];
+  int32_t strips, bands;  // warp items: strips x bands, band-major
+};
+
+// Blur-and-downsample levels (csrc/pyramid.cu).  One entry is one level of
+// one image: src (w x h) -> dst ((w+1)/2 x (h+1)/2), computed in warp items
+// of one strip (32 lanes of source bytes) x kPyrBandRows destination rows.
+// Entries are grouped in phases: every entry of a phase depends only on
+// earlier phases (level l of every image is phase l - 1), and the kernel
+// separates phases with a grid-wide barrier.
+constexpr int kPyrBandRows = 8;
+constexpr int kPyrMaxPhases = 32;
+constexpr int kPyrInline = 8;  // entries carried in the launch parameters
+
+struct PyrEntry {
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride, dst_stride;
+  int32_t w, h, ow, oh;
+  int32_t strips;      // warp strips across a row
+  int32_t main_items;  // strips x bands; the entry's further items are edge tasks
+  int32_t item_end;    // warp items of its phase up to and including this entry
+  int32_t border, border_value;
+};
+
+struct PyrLaunch {
+  const PyrEntry *entries;  // device table, or nullptr: inline_entries
+  PyrEntry inline_entries[kPyrInline];
+  int32_t phase_begin[kPyrMaxPhases + 1];  // entries of phase p: [phase_begin[p], phase_begin[p+1])
+  int32_t phases;
+  int32_t channels;
+  unsigned *barrier;  // zero at launch when phases > 1
+  int *err_flag;      // set when a barrier wait hits its limit
+};
+
 // One entry of a batched work-list: tile (strip, band) of job `job`.
 struct BatchTile {
   uint32_t job;

@@ -56,6 +56,21 @@ cudaError_t launch_fused_batch(const FilterJob &rep, const BatchLaunch &b, int *
                                cudaStream_t stream);
 int fused_batch_blocks_per_sm(const FilterJob &rep, const BatchLaunch &b);
 
+// separable_filter_2d u16 / s16 with 5x5 kernels on one channel
+// (csrc/sep16.cu).  sep16_eligible: the job is of that kind, its addresses
+// allow 16-bit accesses, and (s16) the taps keep every sum exact in fp32.
+bool sep16_eligible(const FilterJob &job);
+cudaError_t launch_sep16(const FilterJob &job, int sm_count, cudaStream_t stream);
+
+// blur_and_downsample_u8 levels (csrc/pyramid.cu): L.phases phases of
+// entries, one launch (cooperative when there is more than one phase; the
+// barrier counter is cleared on the stream first).
+cudaError_t launch_pyramid(const PyrLaunch &L, int sm_count, cudaStream_t stream);
+// Fills one level's entry: src (w x h x channels) -> dst ((w+1)/2 x (h+1)/2)
+// and its warp items (item_end = the entry's own count).
+void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst, int64_t dst_stride, int w,
+               int h, int channels, int border, int border_value);
+
 // Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
 // generated kernel whose weights do not sum to 256).  `scratch` holds the
 // u8 intermediate image: width*channels bytes per row, `scratch_stride`

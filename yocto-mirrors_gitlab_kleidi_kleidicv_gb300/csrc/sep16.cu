@@ -1,0 +1,363 @@
+// separable_filter_2d on one-channel 16-bit images with 5x5 kernels (sm_103a):
+// the u16 entry point and the s16 extension.
+//
+// Arithmetic (kleidicv/src/filters/separable_filter_2d_neon.cpp:140-158 for
+// u16): vertical sums of u16 x u16 products saturating at 2^32 - 1, then the
+// horizontal sum of those times the horizontal taps, saturated to u16.  This
+// kernel computes both passes in fp32, which gives the same outputs:
+//  * u16: every product and partial sum is a non-negative integer.  While
+//    they stay below 2^24 fp32 holds them exactly; a value that reaches 2^24
+//    is rounded to a value that is still >= 2^24, and every later sum that
+//    depends on it (taps >= 0; a zero tap contributes exactly 0) stays above
+//    65535, as the reference's saturated result does.  So min(sum, 65535) is
+//    exact whatever the taps;
+//  * s16 (taps and data signed): the host routes a call here only when
+//    32768 * sum|kx| * sum|ky| <= 2^24, so every product and partial sum of
+//    both passes is an integer of magnitude <= 2^24, held exactly, and no
+//    saturating s32 add of the reference can trigger.
+// Both passes run on element pairs with the paired fp32 operations of sm_100+
+// (__ffma2_rn: per component the same rounding as fmaf).  Conversions avoid
+// the slow integer<->float units: a 16-bit value v becomes
+// the float 2^23 + v by placing its bits under the exponent of 2^23 (s16 is
+// first biased by 2^15 with an xor), and a result r in [0, 65535] (u16, the
+// horizontal sum starting at 2^23) or [-32768, 32767] (s16, + 1.5 * 2^23)
+// keeps r in the low 16 bits of its float.
+//
+// A warp owns a strip of 32 lanes x 8 elements (16 bytes) of a row, of which
+// lanes 1..30 produce output and lanes 0 and 31 only supply the two-element
+// horizontal halo by shuffle, and a band of at most kSep16MaxBand destination
+// rows.  It first requests every source row of the band at once (one 16-byte
+// cp.async per lane and row into its own shared-memory slots: no register
+// holds data in flight, and no other lane reads the slot), then streams down
+// the band: the converted rows of the vertical window (five rows x 8 floats)
+// rotate through statically indexed register slots (the row loop is unrolled
+// by five), and each destination row costs one shared-memory load per lane.
+// The source must be 16-byte aligned (the host sends other calls to the
+// generic kernel).  This pass reads only the lanes whose 8 elements lie
+// inside the row, [0, wf) with wf = 8 * floor(w / 8), and stores only the
+// outputs whose five columns lie inside that span, x in [2, wf - 2).  The
+// other columns (x < 2 and x >= wf - 2) are edge tasks of the same launch,
+// scheduled first: one lane per (row, column), its 25 border-mapped source
+// elements loaded independently, computed with the same operations.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstdlib>
+
+#include "launch.h"
+#include "sepfused.cuh"
+
+namespace kcv {
+
+namespace {
+
+constexpr int kThreads16 = 128;
+constexpr int kWarps16 = kThreads16 / 32;
+constexpr int kLaneElems = 8;
+constexpr int kStripElems = kSep16Lanes * kLaneElems;
+constexpr int kStageRows = kSep16MaxBand + 4;          // source rows of a band
+constexpr int kWarpStageBytes = kStageRows * 32 * 16;  // 9728
+constexpr int kSmem16 = kWarps16 * kWarpStageBytes;    // 38912
+constexpr int kSplitRow = 10;                          // rows [0, 10) are the first copy group
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Element pairs: x[i] = elements (2i, 2i + 1) of the lane.
+template <bool S16>
+__device__ __forceinline__ void to_float2(const uint4 &raw, float2 (&x)[kLaneElems / 2]) {
+  constexpr float bias = S16 ? 8421376.0f : 8388608.0f;  // 2^23 (+ 2^15)
+  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t v = S16 ? (w[i] ^ 0x80008000u) : w[i];
+    const float2 f = make_float2(__uint_as_float(__byte_perm(v, 0x4B000000u, 0x7410)),
+                                 __uint_as_float(__byte_perm(v, 0x4B000000u, 0x7432)));
+    x[i] = __fadd2_rn(f, make_float2(-bias, -bias));
+  }
+}
+
+// Horizontal pass of one element pair from its tap pairs (the taps of both
+// elements, pair by pair); returns the two result words (each a float whose
+// low 16 bits are the result) packed as two 16-bit values.
+template <bool S16>
+__device__ __forceinline__ uint32_t hfinish2(const float2 (&kx)[5], float2 a, float2 b, float2 c, float2 d,
+                                             float2 e) {
+  if constexpr (S16) {
+    float2 acc = __fmul2_rn(kx[0], a);
+    acc = __ffma2_rn(kx[1], b, acc);
+    acc = __ffma2_rn(kx[2], c, acc);
+    acc = __ffma2_rn(kx[3], d, acc);
+    acc = __ffma2_rn(kx[4], e, acc);
+    acc.x = fminf(fmaxf(acc.x, -32768.0f), 32767.0f);
+    acc.y = fminf(fmaxf(acc.y, -32768.0f), 32767.0f);
+    acc = __fadd2_rn(acc, make_float2(12582912.0f, 12582912.0f));  // 1.5 * 2^23 + r
+    return __byte_perm(__float_as_uint(acc.x), __float_as_uint(acc.y), 0x5410);
+  } else {
+    float2 acc = __ffma2_rn(kx[0], a, make_float2(8388608.0f, 8388608.0f));  // 2^23 + sum
+    acc = __ffma2_rn(kx[1], b, acc);
+    acc = __ffma2_rn(kx[2], c, acc);
+    acc = __ffma2_rn(kx[3], d, acc);
+    acc = __ffma2_rn(kx[4], e, acc);
+    // 2^23 + min(sum, 65535)
+    return __byte_perm(__float_as_uint(fminf(acc.x, 8454143.0f)), __float_as_uint(fminf(acc.y, 8454143.0f)),
+                       0x5410);
+  }
+}
+
+// Destination row from the window slots (its source row y - 2 in slot S0,
+// y - 1 in S0 + 1, ... modulo 5).
+template <bool S16, int S0>
+__device__ __forceinline__ uint4 filter_row(const float2 (&win)[5][kLaneElems / 2], const float2 (&kx)[5],
+                                            const float2 (&ky)[5]) {
+  // P[q]: vertical sums of elements (2q - 2, 2q - 1) of the lane; P[0] and
+  // P[5] come from the neighbour lanes.
+  float2 P[6];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    float2 acc = __fmul2_rn(ky[0], win[S0 % 5][m]);
+    acc = __ffma2_rn(ky[1], win[(S0 + 1) % 5][m], acc);
+    acc = __ffma2_rn(ky[2], win[(S0 + 2) % 5][m], acc);
+    acc = __ffma2_rn(ky[3], win[(S0 + 3) % 5][m], acc);
+    P[m + 1] = __ffma2_rn(ky[4], win[(S0 + 4) % 5][m], acc);
+  }
+  P[0] = make_float2(__shfl_up_sync(0xffffffffu, P[4].x, 1), __shfl_up_sync(0xffffffffu, P[4].y, 1));
+  P[5] = make_float2(__shfl_down_sync(0xffffffffu, P[1].x, 1), __shfl_down_sync(0xffffffffu, P[1].y, 1));
+  // Odd taps read the pairs shifted by one element.
+  float2 Q[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) Q[q] = make_float2(P[q].y, P[q + 1].x);
+  uint32_t o[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) o[m] = hfinish2<S16>(kx, P[m], Q[m], P[m + 1], Q[m + 1], P[m + 2]);
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+__host__ __device__ inline int full_span(int w) { return w / kLaneElems * kLaneElems; }
+
+// Edge columns: x < 2 and x >= max(2, wf - 2), inside the row.
+__host__ __device__ inline int edge_left(int w) { return w < 2 ? w : 2; }
+__host__ __device__ inline int edge_right_start(int w) {
+  const int r = full_span(w) - 2;
+  return r > edge_left(w) ? r : edge_left(w);
+}
+__host__ __device__ inline int edge_cols(int w) { return edge_left(w) + (w - edge_right_start(w)); }
+
+// Edge element: destination (y, x) from its 25 border-mapped source
+// elements, with the operations of filter_row.
+template <bool S16>
+__device__ __forceinline__ void edge_element16(const Sep16Job &j, int y, int x) {
+  const uint32_t bv = static_cast<uint32_t>(j.border_value) & 0xFFFFu;
+  const uint16_t *rows[5];
+  int cols[5];
+#pragma unroll
+  for (int d = 0; d < 5; ++d) {
+    const int my = map_index(y + d - 2, j.h, j.border);
+    rows[d] = my < 0 ? nullptr : reinterpret_cast<const uint16_t *>(j.src + static_cast<int64_t>(my) * j.src_stride);
+    cols[d] = map_index(x + d - 2, j.w, j.border);
+  }
+  uint32_t raw[5][5];
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) raw[r][c] = (rows[r] && cols[c] >= 0) ? __ldg(rows[r] + cols[c]) : bv;
+  float2 kx[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) kx[t] = make_float2(j.kx[t], j.kx[t]);
+  float V[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    float x5[5];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      const uint32_t v = S16 ? (raw[r][c] ^ 0x8000u) : raw[r][c];
+      x5[r] = __uint_as_float(v | 0x4B000000u) - (S16 ? 8421376.0f : 8388608.0f);
+    }
+    float acc = j.ky[0] * x5[0];
+    acc = fmaf(j.ky[1], x5[1], acc);
+    acc = fmaf(j.ky[2], x5[2], acc);
+    acc = fmaf(j.ky[3], x5[3], acc);
+    V[c] = fmaf(j.ky[4], x5[4], acc);
+  }
+  // The pair form with the element in both halves.
+  const uint32_t bits = hfinish2<S16>(kx, make_float2(V[0], V[0]), make_float2(V[1], V[1]), make_float2(V[2], V[2]),
+                                      make_float2(V[3], V[3]), make_float2(V[4], V[4]));
+  reinterpret_cast<uint16_t *>(j.dst + static_cast<int64_t>(y) * j.dst_stride)[x] = static_cast<uint16_t>(bits);
+}
+
+template <bool S16>
+__device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int strip, int band, int lane) {
+  const long e0 = static_cast<long>(strip) * kStripElems + kLaneElems * lane - kLaneElems;
+  const int wf = full_span(j.w);
+  const bool fast = e0 >= 0 && e0 + kLaneElems <= wf;
+  // Outputs x in [2, wf - 2) of lanes 1..30.
+  const bool outputs = lane >= 1 && lane <= kSep16Lanes && e0 + kLaneElems > 2 && e0 < wf - 2;
+  const bool full_store =
+      outputs && e0 >= 2 && e0 + kLaneElems <= wf - 2 &&
+      ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 15) == 0;
+  const uint32_t bv2 = (static_cast<uint32_t>(j.border_value) & 0xFFFFu) * 0x00010001u;
+
+  // Band b covers rows [b h / bands, (b + 1) h / bands): at most
+  // kSep16MaxBand rows.
+  const int y0 = static_cast<int>(static_cast<int64_t>(band) * j.h / j.bands);
+  const int y1 = static_cast<int>(static_cast<int64_t>(band + 1) * j.h / j.bands);
+  const int rows = y1 - y0;
+  const int nrows = rows + 4;  // source rows y0 - 2 .. y1 + 1
+  // Request every source row: slot rr of the lane holds row y0 - 2 + rr.
+  const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage + lane));
+#pragma unroll 1
+  for (int rr = 0; rr < nrows; ++rr) {
+    if (rr == kSplitRow) cp_async_commit();
+    const int y = map_index(y0 - 2 + rr, j.h, j.border);
+    if (y >= 0 && fast) {
+      cp_async16(sbase + rr * 32 * 16, j.src + static_cast<int64_t>(y) * j.src_stride + 2 * e0);
+    } else {
+      // A CONSTANT border row, or a lane outside the span (its elements are
+      // read by no stored output).
+      stage[rr * 32 + lane] = y < 0 ? make_uint4(bv2, bv2, bv2, bv2) : make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  cp_async_commit();
+  // The band's edge columns (strips at the row's ends) while the copies fly.
+  if (strip == 0 || strip == j.strips - 1) {
+    const int nl = edge_left(j.w), rs = edge_right_start(j.w);
+    const int lo = strip == 0 ? 0 : nl, hi = strip == j.strips - 1 ? edge_cols(j.w) : nl;
+    const int per_row = hi - lo;
+    for (int k = lane; k < per_row * rows; k += 32) {
+      const int r = k / per_row, i = lo + (k - r * per_row);
+      edge_element16<S16>(j, y0 + r, i < nl ? i : rs + (i - nl));
+    }
+  }
+
+  float2 kx[5], ky[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    kx[t] = make_float2(j.kx[t], j.kx[t]);
+    ky[t] = make_float2(j.ky[t], j.ky[t]);
+  }
+  // Window slot k holds the converted source row rr with rr = k mod 5.
+  float2 win[5][kLaneElems / 2];
+  if (nrows > kSplitRow)
+    cp_async_wait<1>();  // rows [0, kSplitRow) have landed
+  else
+    cp_async_wait<0>();
+#pragma unroll
+  for (int rr = 0; rr < 4; ++rr) to_float2<S16>(stage[rr * 32 + lane], win[rr]);
+  uint8_t *const dcol = j.dst + 2 * e0;
+#pragma unroll 1
+  for (int base = 0; base < rows; base += 5) {
+    if (base > 0) cp_async_wait<0>();  // every row
+    static_for<0, 5>([&](auto sc) {
+      constexpr int S = decltype(sc)::value;
+      constexpr int slot = (S + 4) % 5;  // receives source row rr = base + S + 4
+      if (base + S >= rows) return;  // past the band (the loop ends here)
+      to_float2<S16>(stage[(base + S + 4) * 32 + lane], win[slot]);
+      const uint4 out = filter_row<S16, S>(win, kx, ky);
+      const int oy = y0 + base + S;
+      if (outputs) {
+        uint8_t *d = dcol + static_cast<int64_t>(oy) * j.dst_stride;
+        if (full_store) {
+          *reinterpret_cast<uint4 *>(d) = out;
+        } else {
+          const uint32_t o[4] = {out.x, out.y, out.z, out.w};
+          uint16_t *d16 = reinterpret_cast<uint16_t *>(d);
+#pragma unroll
+          for (int k = 0; k < kLaneElems; ++k)
+            if (e0 + k >= 2 && e0 + k < wf - 2) d16[k] = static_cast<uint16_t>(o[k >> 1] >> (16 * (k & 1)));
+        }
+      }
+    });
+  }
+}
+
+template <bool S16>
+__global__ void __launch_bounds__(kThreads16, 5) sep16_kernel(const __grid_constant__ Sep16Job j) {
+  extern __shared__ __align__(16) uint4 stage16[];
+  // The next call on the stream may start its CTAs as ours finish; it reads
+  // nothing before this grid has completed.
+  launch_dependents();
+  grid_dependency_wait();  // the source may be the previous call's output
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint4 *stage = stage16 + warp * (kWarpStageBytes / 16);
+  // Items go round the CTAs first, so that every SM (the grid is whole
+  // waves of resident CTAs) gets the same number.
+  const int gw = warp * gridDim.x + blockIdx.x;
+  const int nw = gridDim.x * kWarps16;
+  const int items = j.strips * j.bands;
+  for (int t = gw; t < items; t += nw) {
+    const int band = t / j.strips, strip = t - band * j.strips;
+    run_band16<S16>(j, stage, strip, band, lane);
+  }
+}
+
+template <bool S16>
+cudaError_t launch16(Sep16Job &j, int sm_count, cudaStream_t stream) {
+  auto kern = sep16_kernel<S16>;
+  const cudaError_t ea = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem16);
+  if (ea != cudaSuccess) return ea;
+  int occ = 0;
+  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads16, kSmem16);
+  if (err != cudaSuccess) return err;
+  const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
+  const long slots = resident * kWarps16;
+  // As many bands as one item per resident warp allows, none higher than
+  // kSep16MaxBand rows (larger images: several items per warp).
+  j.strips = (j.w + kStripElems - 1) / kStripElems;
+  const long min_bands = (j.h + kSep16MaxBand - 1) / kSep16MaxBand;
+  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, slots / j.strips)));
+  const long items = static_cast<long>(j.strips) * j.bands;
+  const long grid = std::max(1L, std::min(resident, (items + kWarps16 - 1) / kWarps16));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(grid));
+  cfg.blockDim = dim3(kThreads16);
+  cfg.dynamicSmemBytes = kSmem16;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, j);
+}
+
+}  // namespace
+
+bool sep16_eligible(const FilterJob &f) {
+  if ((f.mode != MODE_SEP_U16 && f.mode != MODE_SEP_S16) || f.ksize != 5 || f.channels != 1) return false;
+  // 16-byte copies of source rows; 16-bit destination stores.
+  if (((reinterpret_cast<uintptr_t>(f.src) | static_cast<uintptr_t>(f.src_stride)) & 15) != 0) return false;
+  if (((reinterpret_cast<uintptr_t>(f.dst) | static_cast<uintptr_t>(f.dst_stride)) & 1) != 0) return false;
+  if (f.mode == MODE_SEP_U16) return true;
+  long sx = 0, sy = 0;
+  for (int t = 0; t < 5; ++t) {
+    sx += std::abs(static_cast<long>(f.wx[t]));
+    sy += std::abs(static_cast<long>(f.wy[t]));
+  }
+  return 32768L * sx * sy <= (1L << 24);
+}
+
+cudaError_t launch_sep16(const FilterJob &f, int sm_count, cudaStream_t stream) {
+  Sep16Job j{};
+  j.src = f.src;
+  j.dst = f.dst;
+  j.src_stride = f.src_stride;
+  j.dst_stride = f.dst_stride;
+  j.w = f.width;
+  j.h = f.height;
+  j.border = f.border;
+  j.border_value = f.border_value;
+  for (int t = 0; t < 5; ++t) {
+    j.kx[t] = static_cast<float>(f.wx[t]);
+    j.ky[t] = static_cast<float>(f.wy[t]);
+  }
+  return f.mode == MODE_SEP_S16 ? launch16<true>(j, sm_count, stream) : launch16<false>(j, sm_count, stream);
+}
+
+}  // namespace kcv
