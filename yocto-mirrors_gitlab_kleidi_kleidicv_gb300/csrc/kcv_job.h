@@ -107,6 +107,9 @@ struct Sep16Job {
   int32_t w, h, border, border_value;
   float kx[5], ky[5];
   int32_t strips, bands;  // warp items: strips x bands, band-major
+  int32_t band_q, band_r;  // band b has band_q + (b < band_r) rows
+  int32_t edge_every;      // items t with t % edge_every == 0 compute edge elements:
+  int32_t edge_per;        // passes [t / edge_every * edge_per, + edge_per) of 32
 };
 
 // Blur-and-downsample levels (csrc/pyramid.cu).  One entry is one level of

@@ -36,9 +36,10 @@
 // generic kernel).  This pass reads only the lanes whose 8 elements lie
 // inside the row, [0, wf) with wf = 8 * floor(w / 8), and stores only the
 // outputs whose five columns lie inside that span, x in [2, wf - 2).  The
-// other columns (x < 2 and x >= wf - 2) are edge tasks of the same launch,
-// scheduled first: one lane per (row, column), its 25 border-mapped source
-// elements loaded independently, computed with the same operations.
+// other columns (x < 2 and x >= wf - 2) are edge elements, spread evenly over
+// all items (each warp computes its share while its copies are in flight):
+// one lane per (row, column), its 25 border-mapped source elements loaded
+// independently, computed with the same operations.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -59,10 +60,12 @@ constexpr int kStripElems = kSep16Lanes * kLaneElems;
 constexpr int kStageRows = kSep16MaxBand + 4;          // source rows of a band
 constexpr int kWarpStageBytes = kStageRows * 32 * 16;  // 9728
 constexpr int kSmem16 = kWarps16 * kWarpStageBytes;    // 38912
-constexpr int kSplitRow = 10;                          // rows [0, 10) are the first copy group
+constexpr int kGroups = (kStageRows + 4) / 5;          // copy groups of five rows: 4
 
+// No "memory" clobber: nothing reads the slot before cp_async_wait, which
+// carries it.
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -204,35 +207,62 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
       ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 15) == 0;
   const uint32_t bv2 = (static_cast<uint32_t>(j.border_value) & 0xFFFFu) * 0x00010001u;
 
-  // Band b covers rows [b h / bands, (b + 1) h / bands): at most
-  // kSep16MaxBand rows.
-  const int y0 = static_cast<int>(static_cast<int64_t>(band) * j.h / j.bands);
-  const int y1 = static_cast<int>(static_cast<int64_t>(band + 1) * j.h / j.bands);
-  const int rows = y1 - y0;
+  // Band b has band_q + (b < band_r) rows (at most kSep16MaxBand).
+  const int rows = j.band_q + (band < j.band_r ? 1 : 0);
+  const int y0 = band * j.band_q + min(band, j.band_r);
+  const int y1 = y0 + rows;
   const int nrows = rows + 4;  // source rows y0 - 2 .. y1 + 1
-  // Request every source row: slot rr of the lane holds row y0 - 2 + rr.
+  static_assert(kGroups == 4, "the waits below assume four copy groups");
+  // Request every source row: slot rr of the lane holds row y0 - 2 + rr, in
+  // kGroups copy groups of five rows (rows [5g, 5g + 5); empty groups at the
+  // end), so that the rows are filtered as their group lands.
   const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage + lane));
+  if (fast && y0 >= 2 && y1 + 2 <= j.h) {
+    // Rows inside the image: consecutive.
+    const uint8_t *g = j.src + static_cast<int64_t>(y0 - 2) * j.src_stride + 2 * e0;
+    uint32_t a = sbase;
+    int rr = 0;
+#pragma unroll
+    for (int grp = 0; grp < kGroups; ++grp) {
 #pragma unroll 1
-  for (int rr = 0; rr < nrows; ++rr) {
-    if (rr == kSplitRow) cp_async_commit();
-    const int y = map_index(y0 - 2 + rr, j.h, j.border);
-    if (y >= 0 && fast) {
-      cp_async16(sbase + rr * 32 * 16, j.src + static_cast<int64_t>(y) * j.src_stride + 2 * e0);
-    } else {
-      // A CONSTANT border row, or a lane outside the span (its elements are
-      // read by no stored output).
-      stage[rr * 32 + lane] = y < 0 ? make_uint4(bv2, bv2, bv2, bv2) : make_uint4(0u, 0u, 0u, 0u);
+      for (; rr < min(nrows, 5 * grp + 5); ++rr, a += 32 * 16, g += j.src_stride) cp_async16(a, g);
+      cp_async_commit();
+    }
+  } else {
+    int rr = 0;
+#pragma unroll
+    for (int grp = 0; grp < kGroups; ++grp) {
+#pragma unroll 1
+      for (; rr < min(nrows, 5 * grp + 5); ++rr) {
+        const int y = map_index(y0 - 2 + rr, j.h, j.border);
+        if (y >= 0 && fast) {
+          cp_async16(sbase + rr * 32 * 16, j.src + static_cast<int64_t>(y) * j.src_stride + 2 * e0);
+        } else {
+          // A CONSTANT border row, or a lane outside the span (its elements
+          // are read by no stored output).
+          stage[rr * 32 + lane] = y < 0 ? make_uint4(bv2, bv2, bv2, bv2) : make_uint4(0u, 0u, 0u, 0u);
+        }
+      }
+      cp_async_commit();
     }
   }
-  cp_async_commit();
-  // The band's edge columns (strips at the row's ends) while the copies fly.
-  if (strip == 0 || strip == j.strips - 1) {
-    const int nl = edge_left(j.w), rs = edge_right_start(j.w);
-    const int lo = strip == 0 ? 0 : nl, hi = strip == j.strips - 1 ? edge_cols(j.w) : nl;
-    const int per_row = hi - lo;
-    for (int k = lane; k < per_row * rows; k += 32) {
-      const int r = k / per_row, i = lo + (k - r * per_row);
-      edge_element16<S16>(j, y0 + r, i < nl ? i : rs + (i - nl));
+  // Edge elements (row-major over the edge columns of every row) go in
+  // passes of 32, one lane each, to every edge_every-th item, edge_per
+  // passes each: a few full-width passes per SM, computed while the item's
+  // copies are in flight.
+  {
+    const int t = band * j.strips + strip;
+    if (t % j.edge_every == 0) {
+      const int ne = edge_cols(j.w), nl = edge_left(j.w), rs = edge_right_start(j.w);
+      const int total = ne * j.h;
+      const int p0 = t / j.edge_every * j.edge_per;
+      for (int p = p0; p < p0 + j.edge_per; ++p) {
+        const int k = p * 32 + lane;
+        if (k < total) {
+          const int y = k / ne, i = k - y * ne;
+          edge_element16<S16>(j, y, i < nl ? i : rs + (i - nl));
+        }
+      }
     }
   }
 
@@ -244,25 +274,26 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
   }
   // Window slot k holds the converted source row rr with rr = k mod 5.
   float2 win[5][kLaneElems / 2];
-  if (nrows > kSplitRow)
-    cp_async_wait<1>();  // rows [0, kSplitRow) have landed
-  else
-    cp_async_wait<0>();
+  cp_async_wait<kGroups - 1>();  // group 0: rows 0 .. 4
 #pragma unroll
   for (int rr = 0; rr < 4; ++rr) to_float2<S16>(stage[rr * 32 + lane], win[rr]);
-  uint8_t *const dcol = j.dst + 2 * e0;
+  uint8_t *d = j.dst + static_cast<int64_t>(y0) * j.dst_stride + 2 * e0;
 #pragma unroll 1
   for (int base = 0; base < rows; base += 5) {
-    if (base > 0) cp_async_wait<0>();  // every row
+    // Destination rows base .. base + 4 read source rows up to base + 8:
+    // groups up to base / 5 + 1.
+    switch (base / 5) {
+      case 0: cp_async_wait<kGroups - 2>(); break;
+      case 1: cp_async_wait<kGroups - 3>(); break;
+      default: cp_async_wait<0>(); break;
+    }
     static_for<0, 5>([&](auto sc) {
       constexpr int S = decltype(sc)::value;
       constexpr int slot = (S + 4) % 5;  // receives source row rr = base + S + 4
       if (base + S >= rows) return;  // past the band (the loop ends here)
       to_float2<S16>(stage[(base + S + 4) * 32 + lane], win[slot]);
       const uint4 out = filter_row<S16, S>(win, kx, ky);
-      const int oy = y0 + base + S;
       if (outputs) {
-        uint8_t *d = dcol + static_cast<int64_t>(oy) * j.dst_stride;
         if (full_store) {
           *reinterpret_cast<uint4 *>(d) = out;
         } else {
@@ -273,6 +304,7 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
             if (e0 + k >= 2 && e0 + k < wf - 2) d16[k] = static_cast<uint16_t>(o[k >> 1] >> (16 * (k & 1)));
         }
       }
+      d += j.dst_stride;
     });
   }
 }
@@ -312,7 +344,12 @@ cudaError_t launch16(Sep16Job &j, int sm_count, cudaStream_t stream) {
   j.strips = (j.w + kStripElems - 1) / kStripElems;
   const long min_bands = (j.h + kSep16MaxBand - 1) / kSep16MaxBand;
   j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, slots / j.strips)));
+  j.band_q = j.h / j.bands;
+  j.band_r = j.h % j.bands;
   const long items = static_cast<long>(j.strips) * j.bands;
+  const long passes = (static_cast<long>(edge_cols(j.w)) * j.h + 31) / 32;
+  j.edge_every = static_cast<int32_t>(passes <= items ? items / std::max(passes, 1L) : 1);
+  j.edge_per = static_cast<int32_t>(passes <= items ? 1 : (passes + items - 1) / items);
   const long grid = std::max(1L, std::min(resident, (items + kWarps16 - 1) / kWarps16));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(grid));
@@ -334,6 +371,10 @@ bool sep16_eligible(const FilterJob &f) {
   // 16-byte copies of source rows; 16-bit destination stores.
   if (((reinterpret_cast<uintptr_t>(f.src) | static_cast<uintptr_t>(f.src_stride)) & 15) != 0) return false;
   if (((reinterpret_cast<uintptr_t>(f.dst) | static_cast<uintptr_t>(f.dst_stride)) & 1) != 0) return false;
+  // Item and edge indices in 32 bits.
+  if (static_cast<long>(f.height) * (f.width / kStripElems + 1) >= (1L << 30) ||
+      static_cast<long>(f.height) * 16 >= (1L << 30))
+    return false;
   if (f.mode == MODE_SEP_U16) return true;
   long sx = 0, sy = 0;
   for (int t = 0; t < 5; ++t) {
