@@ -108,6 +108,32 @@ def test_gaussian_arbitrary_weights_not_summing_to_256(kcv, oracle, ctx, k, i):
     check_gaussian(kcv, oracle, ctx, rng, wmin + 1, k - 1, 1, k, sigma, 1, low=250, high=255)
 
 
+@pytest.mark.parametrize("k,sigma", [(3, 0.8), (5, 1.1), (7, 1.5), (7, 2.6)])
+def test_gaussian_four_channel_streaming(kcv, oracle, ctx, k, sigma):
+    """The four-channel streaming Gaussian (16-byte aligned rows): several
+    warp strips and bands, ragged widths (edge pixels on both sides, lanes
+    past the aligned span), minimum sizes, every border and CONSTANT values,
+    aligned and unaligned destinations, and a source 8 bytes off alignment
+    (the generic kernel)."""
+    rng = np.random.default_rng(k * 10 + int(sigma * 10))
+    sizes = [(121, 37), (240, 15), (723, 203), (1999, 64), (k - 1, k - 1), (k + 2, 11), (33, 300)]
+    for i, (w, h) in enumerate(sizes):
+        for border in BORDERS + [0]:
+            pad = (16 - (w * 4) % 16) % 16 + 16  # rows a multiple of 16 bytes
+            host = padded(rng, h, w * 4, np.uint8, pad)
+            bv = int(rng.integers(0, 256)) if border == 0 else None
+            offset = 8 if (i + border) % 4 == 0 else 0
+            got, pad_ok = run_gaussian(kcv, ctx, host, w, h, 4, k, sigma, border, bv=bv, offset=offset,
+                                       dst_pad=pad if border % 2 else 7)
+            err, want = oracle.gaussian_blur_u8(host, w, h, 4, k, sigma, border, ext=bv is not None,
+                                                border_value=bv or 0, nthreads=8)
+            assert err == oracle.OK and pad_ok
+            if not np.array_equal(got, want):
+                bad = np.argwhere(got != want)
+                raise AssertionError(f"{len(bad)} mismatches (w={w} h={h} k={k} s={sigma} b={border} "
+                                     f"off={offset}); first {bad[:4].tolist()}")
+
+
 @pytest.mark.parametrize("offset", [1, 3, 8])
 def test_gaussian_misaligned_and_padded(kcv, oracle, ctx, offset):
     rng = np.random.default_rng(offset)

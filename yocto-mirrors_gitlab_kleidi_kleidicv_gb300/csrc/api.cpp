@@ -498,6 +498,11 @@ kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
         ctx->launches += 1;
         return cuda_status(ctx, launch_pyramid(L, ctx->sm_count, ctx->stream));
       }
+      if (ctx->tune_threads <= 0 && gauss8_eligible(p.fused)) {
+        // Four-channel generated 3x3 / 5x5 / 7x7: the streaming kernel of gauss8.cu.
+        ctx->launches += 1;
+        return cuda_status(ctx, launch_gauss8(p.fused, ctx->sm_count, ctx->stream));
+      }
       if (ctx->tune_threads <= 0 && sep16_eligible(p.fused)) {
         // One-channel 16-bit 5x5: the fp32 streaming kernel of sep16.cu.
         ctx->launches += 1;

@@ -112,6 +112,23 @@ struct Sep16Job {
   int32_t edge_per;        // passes [t / edge_every * edge_per, + edge_per) of 32
 };
 
+// Four-channel u8 Gaussians, 3x3 / 5x5 / 7x7 generated kernels summing to
+// 256 (csrc/gauss8.cu): a warp strip is 32 lanes x 4 pixels, of which
+// kGauss8Lanes lanes produce output; a warp item is (strip, band of at most
+// kGauss8MaxBand destination rows).
+constexpr int kGauss8Lanes = 30;
+constexpr int kGauss8MaxBand = 14;
+
+struct Gauss8Job {
+  const uint8_t *src;
+  uint8_t *dst;
+  int64_t src_stride, dst_stride;  // bytes
+  int32_t w, h, border, border_value;
+  uint32_t w8[7];          // the full kernel (symmetric), K entries
+  int32_t strips, bands;   // warp items: strips x bands, band-major
+  int32_t band_q, band_r;  // band b has band_q + (b < band_r) rows
+};
+
 // Blur-and-downsample levels (csrc/pyramid.cu).  One entry is one level of
 // one image: src (w x h) -> dst ((w+1)/2 x (h+1)/2), computed in warp items
 // of one strip (32 lanes of source bytes) x kPyrBandRows destination rows.

@@ -62,6 +62,12 @@ int fused_batch_blocks_per_sm(const FilterJob &rep, const BatchLaunch &b);
 bool sep16_eligible(const FilterJob &job);
 cudaError_t launch_sep16(const FilterJob &job, int sm_count, cudaStream_t stream);
 
+// gaussian_blur_u8 on four channels with generated 3x3 / 5x5 / 7x7 kernels
+// summing to 256 (csrc/gauss8.cu).  gauss8_eligible: the job is of that kind
+// and its source rows allow 16-byte copies.
+bool gauss8_eligible(const FilterJob &job);
+cudaError_t launch_gauss8(const FilterJob &job, int sm_count, cudaStream_t stream);
+
 // blur_and_downsample_u8 levels (csrc/pyramid.cu): L.phases phases of
 // entries, one launch (cooperative when there is more than one phase; the
 // barrier counter is cleared on the stream first).
