@@ -214,7 +214,7 @@ def measured_hbm_peak():
 def profiled_traffic():
     """dram__bytes_read.sum + dram__bytes_write.sum per launch of the Gaussian
     kernel, from the committed ncu summary (None if absent)."""
-    p = os.path.join(REPO, "profiles", "sepfused_gauss7_rgba_4k.md")
+    p = os.path.join(REPO, "profiles", "gauss8_gauss7_rgba_4k.md")
     try:
         with open(p) as f:
             for line in f:
@@ -1363,7 +1363,7 @@ def main():
         "hbm_gbs": round(world * algorithmic_bytes(calls) / (res["ms_step"] * 1e-3) / 1e9, 1),
         "per_call_us": {c["name"]: round(1e3 * t, 2) for c, t in zip(calls, res["per_call"])},
         "per_call_note": "the Gaussian timed inside the timed region; the others each timed alone afterwards",
-        "roofline": {"kernel": "sepfused_kernel<SIGMA, 7, 4> (gaussian_blur_u8 3840x2160x4 7x7)",
+        "roofline": {"kernel": "gauss8_kernel<7> (gaussian_blur_u8 3840x2160x4 7x7)",
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": f"{peak_kind} hbm_gbs (copy bandwidth)",

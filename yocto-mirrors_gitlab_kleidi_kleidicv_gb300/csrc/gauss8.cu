@@ -300,8 +300,11 @@ cudaError_t launch8(Gauss8Job &j, int sm_count, cudaStream_t stream) {
   const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
   const long slots = resident * kWarpsG;
   j.strips = (j.w + kStripPix - 1) / kStripPix;
+  // Bands of at most kGauss8MaxBand rows, as many as give every resident warp
+  // the same number of items (one wave of n items per warp).
   const long min_bands = (j.h + kGauss8MaxBand - 1) / kGauss8MaxBand;
-  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, slots / j.strips)));
+  const long per_warp = std::max(1L, (min_bands * j.strips + slots - 1) / slots);
+  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, per_warp * slots / j.strips)));
   j.band_q = j.h / j.bands;
   j.band_r = j.h % j.bands;
   const long items = static_cast<long>(j.strips) * j.bands;

@@ -339,11 +339,12 @@ cudaError_t launch16(Sep16Job &j, int sm_count, cudaStream_t stream) {
   if (err != cudaSuccess) return err;
   const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
   const long slots = resident * kWarps16;
-  // As many bands as one item per resident warp allows, none higher than
-  // kSep16MaxBand rows (larger images: several items per warp).
   j.strips = (j.w + kStripElems - 1) / kStripElems;
+  // Bands of at most kSep16MaxBand rows, as many as give every resident warp
+  // the same number of items (one wave of n items per warp).
   const long min_bands = (j.h + kSep16MaxBand - 1) / kSep16MaxBand;
-  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, slots / j.strips)));
+  const long per_warp = std::max(1L, (min_bands * j.strips + slots - 1) / slots);
+  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, per_warp * slots / j.strips)));
   j.band_q = j.h / j.bands;
   j.band_r = j.h % j.bands;
   const long items = static_cast<long>(j.strips) * j.bands;
