@@ -284,7 +284,10 @@ __global__ void __launch_bounds__(kThreadsG, 5) gauss8_kernel(const __grid_const
   const int nw = gridDim.x * kWarpsG;
   const int items = j.strips * j.bands;
   for (int t = gw; t < items; t += nw) {
-    const int band = t / j.strips, strip = t - band * j.strips;
+    // Strips rotate by 7 per band: a warp's items do not all land on the
+    // costlier strips at the row's ends.
+    const int band = t / j.strips, q = t - band * j.strips;
+    const int strip = static_cast<int>((q + 7L * band) % j.strips);
     run_band8<K>(j, stage, strip, band, lane);
   }
 }

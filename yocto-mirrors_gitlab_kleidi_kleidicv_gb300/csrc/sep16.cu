@@ -324,7 +324,10 @@ __global__ void __launch_bounds__(kThreads16, 5) sep16_kernel(const __grid_const
   const int nw = gridDim.x * kWarps16;
   const int items = j.strips * j.bands;
   for (int t = gw; t < items; t += nw) {
-    const int band = t / j.strips, strip = t - band * j.strips;
+    // Strips rotate by 7 per band: a warp's items do not all land on the
+    // costlier strips at the row's ends.
+    const int band = t / j.strips, q = t - band * j.strips;
+    const int strip = static_cast<int>((q + 7L * band) % j.strips);
     run_band16<S16>(j, stage, strip, band, lane);
   }
 }
