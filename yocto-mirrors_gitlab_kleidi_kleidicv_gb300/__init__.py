@@ -383,20 +383,33 @@ def build_pyramid_u8(src, src_stride, src_width, src_height, channels, dsts, dst
                                                ctypes.cast(ds, ctypes.c_void_p), border_type, _h(ctx))
 
 
+class PyramidBatch:
+    """The arguments of one kleidicv_gpu_build_pyramids_u8 call, converted once:
+    pyramids is a list of (src, src_stride, width, height, channels, dsts,
+    dst_strides, border).  launch() makes the call (repeatable)."""
+
+    def __init__(self, pyramids):
+        self.n = len(pyramids)
+        self.arr = (Pyramid * max(self.n, 1))()
+        self._keep = []
+        for i, (src, ss, w, h, c, dsts, dss, border) in enumerate(pyramids):
+            dp = (ctypes.c_void_p * max(len(dsts), 1))(*dsts)
+            ds = (ctypes.c_size_t * max(len(dss), 1))(*dss)
+            self._keep += [dp, ds]
+            self.arr[i] = Pyramid(src, ss, w, h, c, len(dsts), ctypes.cast(dp, _vp), ctypes.cast(ds, _vp),
+                                  border)
+        self.statuses = (_i * max(self.n, 1))()
+
+    def launch(self, ctx=None):
+        """Returns (error, statuses)."""
+        err = lib().kleidicv_gpu_build_pyramids_u8(self.arr, self.n, self.statuses, _h(ctx))
+        return err, list(self.statuses)[:self.n]
+
+
 def build_pyramids_u8(pyramids, ctx=None):
     """pyramids: list of (src, src_stride, width, height, channels, dsts, dst_strides, border).
     Returns (error, statuses)."""
-    n = len(pyramids)
-    arr = (Pyramid * max(n, 1))()
-    keep = []
-    for i, (src, ss, w, h, c, dsts, dss, border) in enumerate(pyramids):
-        dp = (ctypes.c_void_p * max(len(dsts), 1))(*dsts)
-        ds = (ctypes.c_size_t * max(len(dss), 1))(*dss)
-        keep += [dp, ds]
-        arr[i] = Pyramid(src, ss, w, h, c, len(dsts), ctypes.cast(dp, _vp), ctypes.cast(ds, _vp), border)
-    st = (_i * max(n, 1))()
-    err = lib().kleidicv_gpu_build_pyramids_u8(arr, n, st, _h(ctx))
-    return err, list(st)[:n]
+    return PyramidBatch(pyramids).launch(ctx)
 
 
 # --- Lucas-Kanade pyramid ---------------------------------------------------

@@ -441,6 +441,30 @@ kleidicv_error_t cuda_status(kleidicv_gpu_context *ctx, cudaError_t e) {
   return KLEIDICV_GPU_ERROR_CUDA;
 }
 
+cudaError_t upload_async(kleidicv_gpu_context *ctx, void *dst, const void *src, size_t bytes) {
+  if (bytes == 0) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(ctx->upload_mutex);
+  kleidicv_gpu_context::UploadSlot &u = ctx->upload[ctx->upload_next];
+  ctx->upload_next = (ctx->upload_next + 1) % kleidicv_gpu_context::kUploadSlots;
+  cudaError_t e = u.done ? cudaEventSynchronize(u.done) : cudaEventCreateWithFlags(&u.done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  if (u.bytes < bytes) {
+    if (u.host) cudaFreeHost(u.host);
+    u.host = nullptr;
+    u.bytes = 0;
+    e = cudaHostAlloc(&u.host, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      u.host = nullptr;
+      return e;
+    }
+    u.bytes = bytes;
+  }
+  memcpy(u.host, src, bytes);
+  e = cudaMemcpyAsync(dst, u.host, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return e;
+  return cudaEventRecord(u.done, ctx->stream);
+}
+
 void *ctx_alloc(kleidicv_gpu_context *ctx, size_t bytes) {
   int f = ctx->fail_allocs.load();
   while (f > 0) {
@@ -488,7 +512,8 @@ kleidicv_error_t execute(kleidicv_gpu_context *ctx, Prepared &p) {
         // One level: the tiled blur-and-downsample kernel of pyramid.cu.
         PyrLaunch L{};
         pyr_entry(L.inline_entries[0], p.fused.src, p.fused.src_stride, p.fused.dst, p.fused.dst_stride,
-                  p.fused.width, p.fused.height, p.fused.channels, p.fused.border, p.fused.border_value);
+                  p.fused.width, p.fused.height, p.fused.channels, p.fused.border, p.fused.border_value,
+                  pyramid_warps(p.fused.channels, ctx->sm_count));
         L.phase_begin[0] = 0;
         L.phase_begin[1] = 1;
         L.phases = 1;
@@ -582,6 +607,10 @@ kleidicv_error_t kleidicv_gpu_context_destroy(kleidicv_gpu_context_t *ctx) {
   for (cudaEvent_t e : ctx->branch_events) cudaEventDestroy(e);
   if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  for (auto &u : ctx->upload) {
+    if (u.host) cudaFreeHost(u.host);
+    if (u.done) cudaEventDestroy(u.done);
+  }
   cudaFree(ctx->d_err);
   delete ctx;
   return KLEIDICV_OK;
@@ -811,7 +840,7 @@ kleidicv_error_t kleidicv_gpu_build_pyramid_u8(const uint8_t *src, size_t src_st
     for (size_t k = 0; k < n; ++k) {
       const FilterJob &j = p[l0 + k].fused;
       pyr_entry(L.inline_entries[k], j.src, j.src_stride, j.dst, j.dst_stride, j.width, j.height,
-                static_cast<int>(channels), j.border, 0);
+                static_cast<int>(channels), j.border, 0, pyramid_warps(static_cast<int>(channels), ctx->sm_count));
       L.phase_begin[k] = static_cast<int32_t>(k);
     }
     L.phase_begin[n] = static_cast<int32_t>(n);
@@ -864,14 +893,21 @@ kleidicv_error_t kleidicv_gpu_build_pyramids_u8(const kleidicv_gpu_pyramid_t *py
     for (size_t i = 0; i < count; ++i)
       if (static_cast<int>(pyramids[i].channels) == c) phases = std::max(phases, pyramids[i].levels);
     if (phases == 0) continue;
+    const int warps = pyramid_warps(c, ctx->sm_count);
     for (size_t l = 0; l < phases; ++l) {
       L.phase_begin[l] = static_cast<int32_t>(entries.size());
+      // The phase's images share the resident warps: each entry's bands are
+      // sized for its share.
+      int in_phase = 0;
+      for (size_t i = 0; i < count; ++i)
+        if (static_cast<int>(pyramids[i].channels) == c && l < pyramids[i].levels) ++in_phase;
+      const int share = std::max(1, warps / std::max(in_phase, 1));
       int32_t items = 0;
       for (size_t i = 0; i < count; ++i) {
         if (static_cast<int>(pyramids[i].channels) != c || l >= pyramids[i].levels) continue;
         const FilterJob &j = prep[i][l].fused;
         PyrEntry en;
-        pyr_entry(en, j.src, j.src_stride, j.dst, j.dst_stride, j.width, j.height, c, j.border, 0);
+        pyr_entry(en, j.src, j.src_stride, j.dst, j.dst_stride, j.width, j.height, c, j.border, 0, share);
         items += en.item_end;
         en.item_end = items;
         entries.push_back(en);
@@ -889,8 +925,7 @@ kleidicv_error_t kleidicv_gpu_build_pyramids_u8(const kleidicv_gpu_pyramid_t *py
     } else {
       table = static_cast<PyrEntry *>(ctx_alloc(ctx, bytes));
       if (!table) return KLEIDICV_ERROR_ALLOCATION;
-      // From pageable memory: the call returns once the table is staged.
-      cudaError_t ce = cudaMemcpyAsync(table, entries.data(), bytes, cudaMemcpyHostToDevice, ctx->stream);
+      cudaError_t ce = upload_async(ctx, table, entries.data(), bytes);
       if (ce != cudaSuccess) {
         ctx_free(ctx, table, bytes);
         return cuda_status(ctx, ce);

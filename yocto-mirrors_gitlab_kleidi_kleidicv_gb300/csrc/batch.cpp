@@ -259,15 +259,10 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
   p->d_tiles = reinterpret_cast<BatchTile *>(p->dmem + jobs_bytes);
   p->d_next = reinterpret_cast<int *>(p->dmem + jobs_bytes + tiles_bytes);
   for (size_t &off : p->generic_off) off += jobs_bytes + tiles_bytes + next_bytes;
-  cudaError_t ce = cudaSuccess;
-  if (!p->jobs.empty())
-    ce = cudaMemcpyAsync(p->d_jobs, p->jobs.data(), p->jobs.size() * sizeof(FilterJob),
-                         cudaMemcpyHostToDevice, ctx->stream);
-  if (ce == cudaSuccess && !all_tiles.empty())
-    ce = cudaMemcpyAsync(p->d_tiles, all_tiles.data(), all_tiles.size() * sizeof(BatchTile),
-                         cudaMemcpyHostToDevice, ctx->stream);
-  // The host arrays are pageable: make sure the copies have read them.
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  // Through the pinned upload ring: no wait for the stream's earlier work.
+  cudaError_t ce = upload_async(ctx, p->d_jobs, p->jobs.data(), p->jobs.size() * sizeof(FilterJob));
+  if (ce == cudaSuccess)
+    ce = upload_async(ctx, p->d_tiles, all_tiles.data(), all_tiles.size() * sizeof(BatchTile));
   const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() +
                                           ((p->generic.empty() && p->copies.empty()) ? 0 : 1));
   if (ce == cudaSuccess) {

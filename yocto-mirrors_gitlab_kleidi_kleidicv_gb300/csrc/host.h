@@ -54,6 +54,18 @@ struct kleidicv_gpu_context {
   std::deque<kleidicv_gpu_async *> async_queue;
   std::thread async_worker;
   bool async_stop = false;
+  // Host-to-device uploads of small tables (batch plans, pyramid entries):
+  // a ring of grow-only pinned buffers, each reused once the event recorded
+  // after its copy has completed, so no upload waits for the stream to drain.
+  struct UploadSlot {
+    void *host = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+  };
+  static constexpr int kUploadSlots = 8;
+  std::mutex upload_mutex;
+  UploadSlot upload[kUploadSlots];
+  int upload_next = 0;
 };
 
 namespace kcv {
@@ -129,6 +141,10 @@ void shutdown_async(kleidicv_gpu_context *ctx);
 kleidicv_error_t resolve_context(kleidicv_gpu_context *&ctx);
 void *ctx_alloc(kleidicv_gpu_context *ctx, size_t bytes);
 void ctx_free(kleidicv_gpu_context *ctx, void *p, size_t bytes);
+// Copies `bytes` from host memory `src` to device memory `dst` on the
+// context's stream through the pinned upload ring: `src` may be reused as
+// soon as the call returns, and the call does not wait for earlier work.
+cudaError_t upload_async(kleidicv_gpu_context *ctx, void *dst, const void *src, size_t bytes);
 kleidicv_error_t cuda_status(kleidicv_gpu_context *ctx, cudaError_t e);
 
 // Device guard: makes ctx->device current for the calling thread.

@@ -130,11 +130,12 @@ struct Gauss8Job {
 };
 
 // Blur-and-downsample levels (csrc/pyramid.cu).  One entry is one level of
-// one image: src (w x h) -> dst ((w+1)/2 x (h+1)/2), computed in warp items
-// of one strip (32 lanes of source bytes) x kPyrBandRows destination rows.
-// Entries are grouped in phases: every entry of a phase depends only on
-// earlier phases (level l of every image is phase l - 1), and the kernel
-// separates phases with a grid-wide barrier.
+// one image: src (w x h) -> dst ((w+1)/2 x (h+1)/2), computed in warp items:
+// first its edge tasks (32 edge elements each), then (strip of 32 lanes of
+// source bytes, band of at most kPyrBandRows destination rows).  Entries are
+// grouped in phases: every entry of a phase depends only on earlier phases
+// (level l of every image is phase l - 1), and the kernel separates phases
+// with a grid-wide barrier.
 constexpr int kPyrBandRows = 8;
 constexpr int kPyrMaxPhases = 32;
 constexpr int kPyrInline = 8;  // entries carried in the launch parameters
@@ -144,9 +145,10 @@ struct PyrEntry {
   uint8_t *dst;
   int64_t src_stride, dst_stride;
   int32_t w, h, ow, oh;
-  int32_t strips;      // warp strips across a row
-  int32_t main_items;  // strips x bands; the entry's further items are edge tasks
-  int32_t item_end;    // warp items of its phase up to and including this entry
+  int32_t strips, bands;   // band items: strips x bands (none for an unaligned source)
+  int32_t band_q, band_r;  // band b has band_q + (b < band_r) destination rows
+  int32_t edge_items;      // the entry's first items
+  int32_t item_end;        // warp items of its phase up to and including this entry
   int32_t border, border_value;
 };
 

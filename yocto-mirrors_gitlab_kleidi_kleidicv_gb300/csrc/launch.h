@@ -73,9 +73,13 @@ cudaError_t launch_gauss8(const FilterJob &job, int sm_count, cudaStream_t strea
 // barrier counter is cleared on the stream first).
 cudaError_t launch_pyramid(const PyrLaunch &L, int sm_count, cudaStream_t stream);
 // Fills one level's entry: src (w x h x channels) -> dst ((w+1)/2 x (h+1)/2)
-// and its warp items (item_end = the entry's own count).
+// and its warp items (item_end = the entry's own count), its bands sized for
+// `warps` resident warps (pyramid_warps).
 void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst, int64_t dst_stride, int w,
-               int h, int channels, int border, int border_value);
+               int h, int channels, int border, int border_value, int warps);
+// Resident warps of the pyramid kernel for `channels` on `sm_count` SMs (0 on
+// a CUDA failure).
+int pyramid_warps(int channels, int sm_count);
 
 // Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
 // generated kernel whose weights do not sum to 256).  `scratch` holds the

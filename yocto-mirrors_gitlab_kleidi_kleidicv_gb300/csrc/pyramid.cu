@@ -8,33 +8,34 @@
 // Destination size ((w+1)/2, (h+1)/2).
 //
 // A warp owns a strip of 32 lanes x B source bytes (B = 16, or 24 for three
-// channels) and a band of kPyrBandRows destination rows, and streams down the
-// band's 2 * kPyrBandRows + 3 source rows with no shared memory:
-//  * each lane loads its B bytes of a row with vector loads; the few words its
-//    taps need beyond them come from the neighbouring lanes by shuffle (lanes
-//    0 and 31 load them).  Only bytes inside the row are read (word or byte
-//    loads for lanes at the row's ends, and for every lane of a source that
-//    vector loads cannot address), and only destination pixels whose five
-//    source columns lie inside the row are stored: X in [1, (w - 3) / 2];
-//  * horizontal pass: for one to three channels every destination element is
-//    a chain of dp4a over the words its five taps fall in (weights [1 4 6 4 1]
-//    placed at the taps' byte positions, known at compile time); for four
-//    channels the words split into packed 16-bit lanes (channels 0/2 and 1/3)
-//    and the taps are whole words;
+// channels) and a band of at most kPyrBandRows destination rows:
+//  * it requests the band's 2 * rows + 3 source rows at once: the strip's
+//    bytes plus a 16-byte chunk on either side, as 16-byte cp.async chunks
+//    spread over the lanes, into the warp's shared-memory rows, in copy
+//    groups of five rows that are filtered as they land;
+//  * horizontal pass: each lane reads its tap window (its B bytes and the
+//    words around them) from the staged row.  For one to three channels every
+//    destination element is a chain of dp4a over the words its five taps fall
+//    in (weights [1 4 6 4 1] placed at the taps' byte positions, known at
+//    compile time); for four channels the words split into packed 16-bit lanes
+//    (channels 0/2 and 1/3) and the taps are whole words;
 //  * vertical pass: the horizontal sums of the last three source rows stay in
 //    registers as packed 16-bit pairs, and each destination row adds two new
 //    rows: a + e + 4 (b + d) + 6 c + 128 per lane, whose high bytes are the
 //    destination bytes.
-// The source rows of the next destination row are in flight while the
-// current one is computed.  The remaining pixels of each row (X = 0 and the
-// last one or two) are edge tasks of the same phase: one lane per (row,
-// element), its 25 border-mapped source bytes loaded independently.
+// Only 16-byte chunks inside the row are copied (the source must be 16-byte
+// aligned), and only destination pixels whose five source columns lie inside
+// them are stored: X in [1, (wsafe - 3) / 2] with wsafe the pixels of the
+// row's whole chunks.  The remaining pixels of each row (X = 0 and the last
+// few) are edge tasks of the same phase, scheduled first: one lane per (row,
+// element), its 25 border-mapped source bytes loaded independently.  An
+// unaligned source is edge tasks only.
 //
 // A pyramid is one launch: each level of each image is a phase, and phases
 // are separated by a grid-wide barrier (every CTA resident: cooperative
 // launch).  Level l + 1 reads level l right after it was written, mostly from
-// L2, through loads that bypass L1.  Every barrier wait is bounded; on expiry
-// the kernel sets the error flag and returns.
+// L2, through copies and loads that bypass L1.  Every barrier wait is bounded;
+// on expiry the kernel sets the error flag and returns.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -47,9 +48,12 @@ namespace kcv {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
+constexpr int kStageRows = 2 * kPyrBandRows + 3;
+constexpr int kGroups = (kStageRows + 4) / 5;  // copy groups of five rows: 4
 constexpr uint64_t kBarrierLimitNs = 2000000000ull;
+constexpr int kPyrSearchEntries = 512;  // phases with more entries search in global memory
 
 // Lane geometry for C channels.
 template <int C>
@@ -60,7 +64,16 @@ struct LaneGeo {
   static constexpr int NT = HL + NW + 1;      // tap window: HL, own words, one to the right
   static constexpr int OUT = B / 2;           // destination bytes of a lane
   static constexpr int NH = OUT / 2;          // packed 16-bit pairs of sums
+  static constexpr int SPAN = 32 * B;         // strip bytes
+  static constexpr int CHUNKS = SPAN / 16 + 2;  // staged 16-byte chunks of a row: the strip +- 16
+  static constexpr int ROW = CHUNKS * 16;       // staged row bytes
+  static constexpr int WARP_STAGE = kStageRows * ROW;
 };
+
+template <int C>
+constexpr int smem_bytes() {
+  return kWarps * LaneGeo<C>::WARP_STAGE;
+}
 
 // dp4a weight word of window word q (relative to the lane's first word) for
 // destination element j of the lane (one to three channels): the tap weights
@@ -79,40 +92,6 @@ __host__ __device__ constexpr uint32_t tap_word(int c, int j, int q) {
 }
 
 template <bool FRESH>
-__device__ __forceinline__ uint32_t ld32(const uint8_t *p) {
-  uint32_t v;
-  if (FRESH)
-    asm("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
-  else
-    asm("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
-  return v;
-}
-
-template <bool FRESH>
-__device__ __forceinline__ uint2 ld64(const uint8_t *p) {
-  uint2 v;
-  if (FRESH)
-    asm("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
-  else
-    asm("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
-  return v;
-}
-
-template <bool FRESH>
-__device__ __forceinline__ uint4 ld128(const uint8_t *p) {
-  uint4 v;
-  if (FRESH)
-    asm("ld.global.cg.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
-  else
-    asm("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
-  return v;
-}
-
-template <bool FRESH>
 __device__ __forceinline__ uint32_t ld8(const uint8_t *p) {
   uint16_t v;
   if (FRESH)
@@ -120,6 +99,28 @@ __device__ __forceinline__ uint32_t ld8(const uint8_t *p) {
   else
     asm("ld.global.nc.u8 %0, [%1];" : "=h"(v) : "l"(p));
   return v;
+}
+
+// cp.async.cg goes through L2 only: safe for a source written earlier in the
+// same launch.  No "memory" clobber: nothing reads the slot before the wait.
+__device__ __forceinline__ void cp_async16p(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src));
+}
+__device__ __forceinline__ void cp_async_commit_p() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_p() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Waits until at most `pending` copy groups are outstanding, then makes the
+// warp's copies visible to all its lanes.
+__device__ __forceinline__ void wait_groups(int pending) {
+  switch (pending) {
+    case 0: cp_async_wait_p<0>(); break;
+    case 1: cp_async_wait_p<1>(); break;
+    case 2: cp_async_wait_p<2>(); break;
+    default: cp_async_wait_p<3>(); break;
+  }
+  __syncwarp();
 }
 
 __device__ __forceinline__ uint32_t ld_acquire_u32(const unsigned *p) {
@@ -153,98 +154,15 @@ __device__ bool grid_barrier(unsigned *count, unsigned epoch, int *err_flag) {
   return ok != 0;
 }
 
-// Per-lane constants of one (entry, strip).
-struct LaneCtx {
-  const uint8_t *src;
-  int64_t src_stride;
-  long e0;      // first source element (byte) of the lane
-  long wc;      // source row bytes
-  int w, h, border;
-  uint32_t bv;  // CONSTANT border byte
-  bool live;    // the lane's window reaches inside the row
-  bool fast;    // vector loads: aligned source, tap window inside the row
-  bool al4;     // 4-byte aligned source rows
-};
-
-// The tap window of source row r (before border mapping): own words at
-// t[HL ..], the left words at t[0 .. HL-1], the right word at t[NT-1].  Fast
-// lanes other than 0 and 31 leave their left/right words to the shuffle in
-// hsums().  Lanes past the row's end leave t as it is.
-template <int C, bool FRESH>
-__device__ __forceinline__ void load_row(const LaneCtx &lc, int r, int lane, uint32_t (&t)[LaneGeo<C>::NT]) {
-  using G = LaneGeo<C>;
-  const int y = map_index(r, lc.h, lc.border);
-  if (y < 0) {  // a CONSTANT border row: the whole window is the border value
-#pragma unroll
-    for (int k = 0; k < G::NT; ++k) t[k] = lc.bv * 0x01010101u;
-    return;
-  }
-  const uint8_t *row = lc.src + static_cast<int64_t>(y) * lc.src_stride;
-  if (lc.fast) {
-    const uint8_t *p = row + lc.e0;
-    if constexpr (C == 3) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const uint2 v = ld64<FRESH>(p + 8 * k);
-        t[G::HL + 2 * k] = v.x;
-        t[G::HL + 2 * k + 1] = v.y;
-      }
-    } else {
-      const uint4 v = ld128<FRESH>(p);
-      t[G::HL] = v.x;
-      t[G::HL + 1] = v.y;
-      t[G::HL + 2] = v.z;
-      t[G::HL + 3] = v.w;
-    }
-    if (lane == 0) {
-      if constexpr (G::HL == 2) {
-        const uint2 v = ld64<FRESH>(p - 8);
-        t[0] = v.x;
-        t[1] = v.y;
-      } else {
-        t[0] = ld32<FRESH>(p - 4);
-      }
-    } else if (lane == 31) {
-      t[G::NT - 1] = ld32<FRESH>(p + G::B);
-    }
-  } else if (lc.live) {
-    // Lanes at the row's ends and unaligned sources: the window's bytes that
-    // lie inside the row (others 0: no stored pixel reads them), whole words
-    // where possible.
-    const long x0 = lc.e0 - 4 * G::HL;
-#pragma unroll
-    for (int k = 0; k < G::NT; ++k) {
-      const long x = x0 + 4 * k;
-      if (lc.al4 && x >= 0 && x + 4 <= lc.wc) {
-        t[k] = ld32<FRESH>(row + x);
-      } else {
-        uint32_t b[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) b[i] = (x + i >= 0 && x + i < lc.wc) ? ld8<FRESH>(row + x + i) : 0u;
-        t[k] = b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
-      }
-    }
-  }
-}
-
-// Horizontal sums of one source row for the lane's OUT destination elements,
-// as NH packed 16-bit pairs (sums <= 4080).
+// Horizontal sums of one staged source row for the lane's OUT destination
+// elements, as NH packed 16-bit pairs (sums <= 4080).  `row` is the staged
+// row, `off` the byte offset of the lane's tap window in it.
 template <int C>
-__device__ __forceinline__ void hsums(const LaneCtx &lc, int lane, uint32_t (&t)[LaneGeo<C>::NT],
-                                      uint32_t (&hs)[LaneGeo<C>::NH]) {
+__device__ __forceinline__ void hsums(const uint8_t *row, int off, uint32_t (&hs)[LaneGeo<C>::NH]) {
   using G = LaneGeo<C>;
-  // Neighbour words: the left lane's last HL words, the right lane's first.
-  uint32_t up[G::HL];
+  uint32_t t[G::NT];
 #pragma unroll
-  for (int k = 0; k < G::HL; ++k) up[k] = __shfl_up_sync(0xffffffffu, t[G::NW + k], 1);
-  const uint32_t dn = __shfl_down_sync(0xffffffffu, t[G::HL], 1);
-  if (lc.fast) {
-    if (lane != 0) {
-#pragma unroll
-      for (int k = 0; k < G::HL; ++k) t[k] = up[k];
-    }
-    if (lane != 31) t[G::NT - 1] = dn;
-  }
+  for (int k = 0; k < G::NT; ++k) t[k] = *reinterpret_cast<const uint32_t *>(row + off + 4 * k);
   if constexpr (C == 4) {
     // Window word k is pixel k - 2 of the lane; destination pixel m is
     // centred on pixel 2m: its taps are words 2m .. 2m + 4.
@@ -277,68 +195,72 @@ __device__ __forceinline__ void hsums(const LaneCtx &lc, int lane, uint32_t (&t)
   }
 }
 
-// One band (kPyrBandRows destination rows) of one strip of one entry.
-template <int C, bool FRESH>
-__device__ __forceinline__ void run_band(const PyrEntry &e, int strip, int band, int lane) {
-  using G = LaneGeo<C>;
-  LaneCtx lc;
-  lc.src = e.src;
-  lc.src_stride = e.src_stride;
-  lc.w = e.w;
-  lc.h = e.h;
-  lc.border = e.border;
-  lc.bv = static_cast<uint32_t>(e.border_value) & 0xFFu;
-  lc.wc = static_cast<long>(e.w) * C;
-  lc.e0 = (static_cast<long>(strip) * 32 + lane) * G::B;
-  lc.live = lc.e0 - 4 * G::HL < lc.wc;
-  const uintptr_t sa = reinterpret_cast<uintptr_t>(e.src) | static_cast<uintptr_t>(e.src_stride);
-  lc.al4 = (sa & 3) == 0;
-  lc.fast = (sa & (C == 3 ? 7 : 15)) == 0 && lc.e0 >= 4 * G::HL && lc.e0 + G::B + 4 <= lc.wc;
+// Last interior destination pixel of a level (0: none): its five source
+// columns lie inside the row's whole 16-byte chunks.
+__host__ __device__ inline int interior_last(int w, int c, bool aligned) {
+  if (!aligned) return 0;
+  const int wsafe = static_cast<int>((static_cast<long>(w) * c / 16 * 16) / c);
+  return wsafe >= 3 ? (wsafe - 3) / 2 : 0;
+}
 
-  // Stored: destination elements of pixels [1, (w - 3) / 2].
-  const long oe = lc.e0 / 2;  // first destination element of the lane
-  const long olo = C, ohi = e.w >= 3 ? static_cast<long>((e.w - 3) / 2 + 1) * C : 0;
+// One band of one strip of one entry.
+template <int C, bool FRESH>
+__device__ __forceinline__ void run_band(const PyrEntry &e, uint8_t *stage, int strip, int band, int lane) {
+  using G = LaneGeo<C>;
+  const long wc = static_cast<long>(e.w) * C;
+  const long base = static_cast<long>(strip) * G::SPAN - 16;  // row byte of staged chunk 0
+  const long e0 = static_cast<long>(strip) * G::SPAN + static_cast<long>(lane) * G::B;
+  const int off = static_cast<int>(e0 - 4 * G::HL - base);  // lane's tap window in the staged row
+  const uint32_t bv4 = (static_cast<uint32_t>(e.border_value) & 0xFFu) * 0x01010101u;
+
+  const int rows = e.band_q + (band < e.band_r ? 1 : 0);
+  const int Y0 = band * e.band_q + min(band, e.band_r);
+  const int nrows = 2 * rows + 3;  // source rows 2 Y0 - 2 .. 2 Y1
+
+  // Copies: row rr of the stage holds source row 2 Y0 - 2 + rr; each lane
+  // copies chunks lane and lane + 32 of it, the chunks inside the row.
+  const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage));
+  int rr = 0;
+#pragma unroll
+  for (int grp = 0; grp < kGroups; ++grp) {
+#pragma unroll 1
+    for (; rr < min(nrows, 5 * grp + 5); ++rr) {
+      const int y = map_index(2 * Y0 - 2 + rr, e.h, e.border);
+#pragma unroll
+      for (int k = lane; k < G::CHUNKS; k += 32) {
+        const long x = base + 16L * k;
+        if (y < 0) {
+          *reinterpret_cast<uint4 *>(stage + rr * G::ROW + 16 * k) = make_uint4(bv4, bv4, bv4, bv4);
+        } else if (x >= 0 && x + 16 <= wc) {
+          cp_async16p(sbase + rr * G::ROW + 16 * k, e.src + static_cast<int64_t>(y) * e.src_stride + x);
+        }
+      }
+    }
+    cp_async_commit_p();
+  }
+
+  // Stored: destination elements of pixels [1, xr].
+  const long oe = e0 / 2;  // first destination element of the lane
+  const long olo = C, ohi = static_cast<long>(interior_last(e.w, C, true) + 1) * C;
   const bool stores = oe + G::OUT > olo && oe < ohi;
   const uintptr_t smask = C == 3 ? 3 : 7;
   const bool full_store =
       oe >= olo && oe + G::OUT <= ohi &&
       ((reinterpret_cast<uintptr_t>(e.dst) | static_cast<uintptr_t>(e.dst_stride)) & smask) == 0;
 
-  const int Y0 = band * kPyrBandRows;
-  const int Y1 = min(Y0 + kPyrBandRows, e.oh);
-  // Horizontal sums of source rows 2Y - 2, 2Y - 1, 2Y (a, b, c) and the raw
-  // windows of rows 2Y + 1, 2Y + 2 (r1, r2).
   uint32_t a[G::NH], b[G::NH], c[G::NH];
-  uint32_t r1[G::NT], r2[G::NT];
-#pragma unroll
-  for (int k = 0; k < G::NT; ++k) r1[k] = r2[k] = 0;
-  {
-    uint32_t s0[G::NT], s1[G::NT], s2[G::NT];
-#pragma unroll
-    for (int k = 0; k < G::NT; ++k) s0[k] = s1[k] = s2[k] = 0;
-    load_row<C, FRESH>(lc, 2 * Y0 - 2, lane, s0);
-    load_row<C, FRESH>(lc, 2 * Y0 - 1, lane, s1);
-    load_row<C, FRESH>(lc, 2 * Y0, lane, s2);
-    load_row<C, FRESH>(lc, 2 * Y0 + 1, lane, r1);
-    load_row<C, FRESH>(lc, 2 * Y0 + 2, lane, r2);
-    hsums<C>(lc, lane, s0, a);
-    hsums<C>(lc, lane, s1, b);
-    hsums<C>(lc, lane, s2, c);
-  }
+  wait_groups(kGroups - 1);  // group 0: rows 0 .. 4
+  hsums<C>(stage, off, a);
+  hsums<C>(stage + G::ROW, off, b);
+  hsums<C>(stage + 2 * G::ROW, off, c);
   uint8_t *drow = e.dst + static_cast<int64_t>(Y0) * e.dst_stride + oe;
 #pragma unroll 1
-  for (int Y = Y0; Y < Y1; ++Y) {
-    // The next destination row's two source rows are in flight meanwhile.
-    uint32_t n1[G::NT], n2[G::NT];
-#pragma unroll
-    for (int k = 0; k < G::NT; ++k) n1[k] = n2[k] = 0;
-    if (Y + 1 < Y1) {
-      load_row<C, FRESH>(lc, 2 * Y + 3, lane, n1);
-      load_row<C, FRESH>(lc, 2 * Y + 4, lane, n2);
-    }
+  for (int r = 0; r < rows; ++r) {
+    // Destination row r reads stage rows 2r + 3 and 2r + 4: group (2r + 4) / 5.
+    wait_groups(max(0, kGroups - 1 - (2 * r + 4) / 5));
     uint32_t d[G::NH], ee[G::NH];
-    hsums<C>(lc, lane, r1, d);
-    hsums<C>(lc, lane, r2, ee);
+    hsums<C>(stage + (2 * r + 3) * G::ROW, off, d);
+    hsums<C>(stage + (2 * r + 4) * G::ROW, off, ee);
     uint32_t s[G::NH];
 #pragma unroll
     for (int k = 0; k < G::NH; ++k) s[k] = a[k] + ee[k] + 0x00800080u + 4u * (b[k] + d[k]) + 6u * c[k];
@@ -370,20 +292,19 @@ __device__ __forceinline__ void run_band(const PyrEntry &e, int strip, int band,
       b[k] = d[k];
       c[k] = ee[k];
     }
-#pragma unroll
-    for (int k = 0; k < G::NT; ++k) {
-      r1[k] = n1[k];
-      r2[k] = n2[k];
-    }
   }
+  // The stage is rewritten by the warp's next item only after every lane
+  // has read it.
+  __syncwarp();
 }
 
 // Edge task `task` of entry e: destination element (Y, X, ch) for the edge
-// pixels X = 0 and X in [max(1, (w - 3) / 2 + 1), ow).
+// pixels X = 0 and X in [max(1, xr + 1), ow).
 template <int C, bool FRESH>
 __device__ __forceinline__ void edge_task(const PyrEntry &e, int task) {
-  const int xr = e.w >= 3 ? (e.w - 3) / 2 : 0;  // last interior pixel (0: none)
-  const int xs = xr + 1 > 1 ? xr + 1 : 1;       // first right-edge pixel
+  const bool aligned = ((reinterpret_cast<uintptr_t>(e.src) | static_cast<uintptr_t>(e.src_stride)) & 15) == 0;
+  const int xr = interior_last(e.w, C, aligned);
+  const int xs = xr + 1 > 1 ? xr + 1 : 1;  // first right-edge pixel
   const int per_row = C * (1 + (e.ow > xs ? e.ow - xs : 0));
   if (task >= per_row * e.oh) return;
   const int Y = task / per_row, q = task - Y * per_row;
@@ -414,51 +335,75 @@ __device__ __forceinline__ void edge_task(const PyrEntry &e, int task) {
   e.dst[static_cast<int64_t>(Y) * e.dst_stride + static_cast<long>(X) * C + ch] = static_cast<uint8_t>(sum >> 8);
 }
 
+template <int C, bool FRESH>
+__device__ __forceinline__ void run_item(const PyrEntry &en, uint8_t *stage, int local, int lane) {
+  if (local < en.edge_items) {
+    edge_task<C, FRESH>(en, local * 32 + lane);
+  } else {
+    // Strips rotate by 7 per band: a warp's items do not all land on the
+    // strips at the row's ends.
+    const int m = local - en.edge_items;
+    const int band = m / en.strips, q = m - band * en.strips;
+    run_band<C, FRESH>(en, stage, static_cast<int>((q + 7L * band) % en.strips), band, lane);
+  }
+}
+
 template <int C>
 __global__ void __launch_bounds__(kThreads) pyramid_kernel(const __grid_constant__ PyrLaunch L) {
+  extern __shared__ __align__(16) uint8_t pyr_stage[];
   launch_dependents();
   grid_dependency_wait();  // the source may be the previous call's output
   const PyrEntry *E = L.entries ? L.entries : L.inline_entries;
-  const int lane = threadIdx.x & 31;
-  const int gwarp = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint8_t *stage = pyr_stage + warp * LaneGeo<C>::WARP_STAGE;
+  // Items go round the CTAs first, so that every SM gets the same number.
+  const int gwarp = warp * gridDim.x + blockIdx.x;
   const int nwarps = gridDim.x * kWarps;
+  // The phase's item boundaries, for the entry search (a table in global
+  // memory would make every search a chain of dependent loads).
+  __shared__ int ends[kPyrSearchEntries];
   for (int ph = 0; ph < L.phases; ++ph) {
     if (ph > 0 && !grid_barrier(L.barrier, static_cast<unsigned>(ph), L.err_flag)) return;
     const int e0 = L.phase_begin[ph], e1 = L.phase_begin[ph + 1];
+    const bool cached = e1 - e0 <= kPyrSearchEntries;
+    __syncthreads();  // the previous phase's readers of ends[] are done
+    if (cached)
+      for (int k = threadIdx.x; k < e1 - e0; k += blockDim.x) ends[k] = E[e0 + k].item_end;
+    __syncthreads();
     const int total = E[e1 - 1].item_end;
     for (int t = gwarp; t < total; t += nwarps) {
       // The entry holding item t: the first with item_end > t.
       int lo = e0, hi = e1 - 1;
       while (lo < hi) {
         const int mid = (lo + hi) / 2;
-        if (E[mid].item_end > t) hi = mid;
+        if ((cached ? ends[mid - e0] : E[mid].item_end) > t) hi = mid;
         else lo = mid + 1;
       }
-      const PyrEntry &en = E[lo];
-      const int local = t - (lo > e0 ? E[lo - 1].item_end : 0);
-      if (local < en.main_items) {
-        const int band = local / en.strips, strip = local - band * en.strips;
-        if (ph == 0)
-          run_band<C, false>(en, strip, band, lane);
-        else
-          run_band<C, true>(en, strip, band, lane);
-      } else {
-        const int task = (local - en.main_items) * 32 + lane;
-        if (ph == 0)
-          edge_task<C, false>(en, task);
-        else
-          edge_task<C, true>(en, task);
-      }
+      const PyrEntry en = E[lo];  // one round of loads, then registers
+      const int local = t - (lo > e0 ? (cached ? ends[lo - 1 - e0] : E[lo - 1].item_end) : 0);
+      if (ph == 0)
+        run_item<C, false>(en, stage, local, lane);
+      else
+        run_item<C, true>(en, stage, local, lane);
     }
   }
 }
 
 template <int C>
+int warps_c(int sm_count) {
+  auto kern = pyramid_kernel<C>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes<C>()) != cudaSuccess)
+    return 0;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, smem_bytes<C>()) != cudaSuccess) return 0;
+  return std::max(occ, 1) * std::max(sm_count, 1) * kWarps;
+}
+
+template <int C>
 cudaError_t launch_c(const PyrLaunch &L, int sm_count, cudaStream_t stream) {
   auto kern = pyramid_kernel<C>;
-  int occ = 0;
-  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, 0);
-  if (err != cudaSuccess) return err;
+  const int warps = warps_c<C>(sm_count);
+  if (warps == 0) return cudaErrorInvalidValue;
   const PyrEntry *E = L.entries ? nullptr : L.inline_entries;
   long most = 1;
   if (E) {
@@ -467,12 +412,11 @@ cudaError_t launch_c(const PyrLaunch &L, int sm_count, cudaStream_t stream) {
   } else {
     most = 1L << 40;  // device table: the caller sized the phases
   }
-  const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
-  const int grid = static_cast<int>(std::max(1L, std::min(resident, (most + kWarps - 1) / kWarps)));
+  const int grid = static_cast<int>(std::max(1L, std::min<long>(warps / kWarps, (most + kWarps - 1) / kWarps)));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(static_cast<unsigned>(grid));
   cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem_bytes<C>();
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   if (L.phases > 1) {
@@ -490,6 +434,16 @@ cudaError_t launch_c(const PyrLaunch &L, int sm_count, cudaStream_t stream) {
 
 }  // namespace
 
+int pyramid_warps(int channels, int sm_count) {
+  switch (channels) {
+    case 1: return warps_c<1>(sm_count);
+    case 2: return warps_c<2>(sm_count);
+    case 3: return warps_c<3>(sm_count);
+    case 4: return warps_c<4>(sm_count);
+  }
+  return 0;
+}
+
 cudaError_t launch_pyramid(const PyrLaunch &L, int sm_count, cudaStream_t stream) {
   if (L.phases > 1) {
     const cudaError_t e = cudaMemsetAsync(L.barrier, 0, sizeof(unsigned), stream);
@@ -505,7 +459,7 @@ cudaError_t launch_pyramid(const PyrLaunch &L, int sm_count, cudaStream_t stream
 }
 
 void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst, int64_t dst_stride, int w,
-               int h, int channels, int border, int border_value) {
+               int h, int channels, int border, int border_value, int warps) {
   e.border = border;
   e.border_value = border_value;
   e.src = src;
@@ -516,16 +470,29 @@ void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst
   e.h = h;
   e.ow = (w + 1) / 2;
   e.oh = (h + 1) / 2;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(src) | static_cast<uintptr_t>(src_stride)) & 15) == 0;
   // A strip makes 32 lanes x (8, or 12 for three channels) destination bytes.
   const long strip_out = 32L * (channels == 3 ? 12 : 8);
   const long owc = static_cast<long>(e.ow) * channels;
-  e.strips = static_cast<int32_t>((owc + strip_out - 1) / strip_out);
-  e.main_items = e.strips * ((e.oh + kPyrBandRows - 1) / kPyrBandRows);
-  // Edge pixels per destination row: X = 0 and X >= max(1, (w - 3) / 2 + 1).
-  const int xr = w >= 3 ? (w - 3) / 2 : 0;
+  e.strips = aligned ? static_cast<int32_t>((owc + strip_out - 1) / strip_out) : 0;
+  // Bands of at most kPyrBandRows rows, as many as give every warp the same
+  // number of items.
+  long bands = 0;
+  if (e.strips > 0) {
+    const long min_bands = (e.oh + kPyrBandRows - 1) / kPyrBandRows;
+    const long slots = std::max(warps, 1);
+    const long per_warp = std::max(1L, (min_bands * e.strips + slots - 1) / slots);
+    bands = std::min<long>(e.oh, std::max(min_bands, per_warp * slots / e.strips));
+  }
+  e.bands = static_cast<int32_t>(bands);
+  e.band_q = bands > 0 ? static_cast<int32_t>(e.oh / bands) : 0;
+  e.band_r = bands > 0 ? static_cast<int32_t>(e.oh % bands) : 0;
+  // Edge pixels per destination row: X = 0 and X >= max(1, xr + 1).
+  const int xr = interior_last(w, channels, aligned);
   const int xs = xr + 1 > 1 ? xr + 1 : 1;
   const long per_row = static_cast<long>(channels) * (1 + (e.ow > xs ? e.ow - xs : 0));
-  e.item_end = e.main_items + static_cast<int32_t>((per_row * e.oh + 31) / 32);
+  e.edge_items = static_cast<int32_t>((per_row * e.oh + 31) / 32);
+  e.item_end = e.edge_items + static_cast<int32_t>(e.strips * bands);
 }
 
 }  // namespace kcv
