@@ -273,7 +273,7 @@ __device__ __forceinline__ void band_loop8(const Gauss8Job &j, const uint4 *stag
 }
 
 template <int K>
-__global__ void __launch_bounds__(kThreadsG, 5) gauss8_kernel(const __grid_constant__ Gauss8Job j) {
+__global__ void __launch_bounds__(kThreadsG, K == 7 ? 4 : 5) gauss8_kernel(const __grid_constant__ Gauss8Job j) {
   extern __shared__ __align__(16) uint4 stage8[];
   launch_dependents();
   grid_dependency_wait();  // the source may be the previous call's output
