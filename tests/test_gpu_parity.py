@@ -414,6 +414,55 @@ def test_pyramids_batched_one_launch(kcv, oracle, ctx):
     assert err == kcv.NOT_IMPLEMENTED and st == [kcv.OK, kcv.NOT_IMPLEMENTED]
 
 
+def test_pyramids_batched_more_entries_than_the_shared_search(kcv, oracle, ctx):
+    """600 small pyramids in one call: a phase with more entries than the
+    kernel keeps in shared memory for its entry search (the search then reads
+    the table in global memory)."""
+    rng = np.random.default_rng(79)
+    cases, expect, keep = [], [], []
+    for i in range(600):
+        w, h = int(rng.integers(8, 40)), int(rng.integers(8, 30))
+        levels = int(rng.integers(1, 3))
+        host = padded(rng, h, w, np.uint8, 16 - w % 16)
+        buf, sp, ss = device_image(torch, host)
+        sizes = pyr_sizes(w, h, levels)
+        outs = [device_output(torch, lh, lw, np.uint8, 0) for (lw, lh) in sizes]
+        keep += [buf, outs]
+        cases.append((sp, ss, w, h, 1, [o[1] for o in outs], [o[2] for o in outs], 4))
+        expect.append((host, w, h, levels, sizes, outs))
+    err, st = kcv.build_pyramids_u8(cases, ctx)
+    assert err == kcv.OK and st == [kcv.OK] * len(cases)
+    assert ctx.synchronize() == kcv.OK
+    for host, w, h, levels, sizes, outs in expect:
+        for (ow, oh), (buf, _p, stv), want in zip(sizes, outs, _pyramid_levels(oracle, host, w, h, 1, levels, 4)):
+            got, _ = read_output(buf, oh, ow, np.uint8, stv)
+            assert np.array_equal(got, want), (w, h)
+
+
+@pytest.mark.parametrize("dt", ["u16", "s16"])
+def test_separable_16bit_tall_image(kcv, oracle, ctx, dt):
+    """70001 rows: more bands than a wave of resident warps holds, several
+    items per warp."""
+    dtype = SEP_DT[dt]
+    rng = np.random.default_rng(81)
+    w, h = 248, 70001
+    host = padded(rng, h, w, dtype, 8)
+    kx = rng.integers(0, 5, 5) if dt == "u16" else rng.integers(-4, 5, 5)
+    ky = rng.integers(0, 5, 5) if dt == "u16" else rng.integers(-4, 5, 5)
+    got, pad_ok = run_separable(kcv, ctx, dt, host, w, h, 1, kx, ky, 3, dst_pad=8)
+    err, want = oracle.separable_filter_2d(host, w, h, 1, kx.astype(dtype), ky.astype(dtype), 3, nthreads=8)
+    assert err == oracle.OK and pad_ok and np.array_equal(got, want)
+
+
+def test_gaussian_four_channel_tall_image(kcv, oracle, ctx):
+    rng = np.random.default_rng(82)
+    w, h = 36, 70001
+    host = padded(rng, h, w * 4, np.uint8, 16)
+    got, pad_ok = run_gaussian(kcv, ctx, host, w, h, 4, 7, 1.5, 4, dst_pad=16)
+    err, want = oracle.gaussian_blur_u8(host, w, h, 4, 7, 1.5, 4, nthreads=8)
+    assert err == oracle.OK and pad_ok and np.array_equal(got, want)
+
+
 def test_blur_and_downsample_tiled_and_pyramid_kernels_agree(kcv, ctx):
     """A forced tile shape selects the tiled stencil; both kernels give the
     same bytes."""
