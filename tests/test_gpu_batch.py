@@ -68,7 +68,7 @@ def _prepare(cases, rng):
         else:
             dtype, ow, oh = np.uint8, (s["w"] + 1) // 2, (s["h"] + 1) // 2
         info = np.iinfo(dtype)
-        host = rng.integers(info.min, int(info.max) + 1, (s["h"], s["w"] * s["c"] + 5), dtype=dtype)
+        host = rng.integers(info.min, int(info.max) + 1, (s["h"], s["w"] * s["c"] + s.get("pad", 5)), dtype=dtype)
         sbuf, sptr, sstride = device_image(torch, host)
         dbuf, dptr, dstride = device_output(torch, oh, ow * s["c"], dtype, pad_elems=3)
         if op == "gauss":
@@ -188,3 +188,28 @@ def test_uneven_batch_512_all_outputs():
     plan.close()
     ctx.close()
     assert not bad, f"{len(bad)} of 512 outputs differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_of_downsamples_pyramid_tables(use_graph):
+    """A plan of blur-and-downsample requests only (one pyramid-kernel launch
+    per channel count over a device entry table): 70 requests of every
+    channel count and border, aligned and unaligned sources, odd sizes down
+    to 1x1, on two launches."""
+    rng = np.random.default_rng(31)
+    cases = []
+    for i in range(70):
+        w, c = (int(rng.integers(1, 900)) if i % 9 else 1), int(rng.integers(1, 5))
+        pad = (-(w * c)) % 16 if i % 2 else 5  # odd requests: 16-byte rows (the kernel's staged strips)
+        cases.append(("bd", dict(w=w, h=int(rng.integers(1, 300)), c=c, border=int(rng.choice(FIXED)), ext=False,
+                                 bv=0, pad=pad)))
+    items = _prepare(cases, rng)
+    ctx = kcv.Context.for_torch(0)
+    plan = kcv.BatchPlan([it["req"] for it in items], ctx)
+    for _ in range(2):
+        _refill(items)
+        assert plan.launch(use_graph) == kcv.OK
+        assert ctx.synchronize() == kcv.OK
+        _check(items, plan.statuses)
+    plan.close()
+    ctx.close()

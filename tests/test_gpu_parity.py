@@ -250,6 +250,32 @@ def test_blur_and_downsample(kcv, oracle, ctx, c):
             assert np.array_equal(got, want), (c, border, w, h)
 
 
+@pytest.mark.parametrize("c", [1, 2, 3, 4])
+def test_blur_and_downsample_unaligned_rows(kcv, oracle, ctx, c):
+    """Unaligned sources take the staged path: every row misaligned by the
+    same amount (aligned stride, base offset 1..15) or by a different amount
+    (odd stride), widths over several strips and below one, every border."""
+    rng = np.random.default_rng(40 + c)
+    for border in BORDERS + [0]:
+        for (w, h, offset, pad) in [(1500, 70, 0, 3), (1536, 41, 5, 0), (263, 9, 7, 9), (3001, 23, 15, 1),
+                                    (40, 33, 3, 5), (17, 4, 1, 0)]:
+            if pad == 0:
+                pad = (-(w * c)) % 16  # 16-byte rows: only the base is unaligned
+            host = padded(rng, h, w * c, np.uint8, pad)
+            ow, oh = (w + 1) // 2, (h + 1) // 2
+            _k, sp, ss = device_image(torch, host, offset)
+            obuf, dp, ds = device_output(torch, oh, ow * c, np.uint8, 5)
+            bv = 17 if border == 0 else None
+            err = kcv.blur_and_downsample_u8(sp, ss, w, h, dp, ds, c, border, ctx, border_value=bv)
+            assert err == kcv.OK
+            assert ctx.synchronize() == kcv.OK
+            got, pad_ok = read_output(obuf, oh, ow * c, np.uint8, ds)
+            e2, want = oracle.blur_and_downsample_u8(host, w, h, c, border, ext=bv is not None,
+                                                     border_value=bv or 0)
+            assert e2 == 0 and pad_ok
+            assert np.array_equal(got, want), (c, border, w, h, offset, pad)
+
+
 def test_pyramid_five_levels(kcv, oracle, ctx):
     rng = np.random.default_rng(9)
     for (w, h, c) in [(515, 301, 1), (200, 131, 3), (128, 96, 4)]:

@@ -8,10 +8,11 @@
 // (mode, size, channels), orders each group's tiles largest first, and
 // uploads the job table and the work-lists in one device allocation.  A
 // launch resets the work counters and starts one persistent kernel per group
-// on forked streams, so the groups run concurrently; arbitrary-size Gaussians
-// (two-pass kernel with a scratch image) and copies run on a branch of their
-// own.  With use_graph the whole launch is captured once into a CUDA graph and
-// replayed.
+// on forked streams, so the groups run concurrently; blur-and-downsample
+// requests go to the pyramid kernel (one launch per channel count over an
+// entry table), and arbitrary-size Gaussians (two-pass kernel with a scratch
+// image) and copies run on a branch of their own.  With use_graph the whole
+// launch is captured once into a CUDA graph and replayed.
 #include <string.h>
 
 #include <algorithm>
@@ -95,6 +96,10 @@ using namespace kcv;
 
 struct kleidicv_gpu_batch_plan {
   kleidicv_gpu_context *ctx = nullptr;
+  // Blur-and-downsample requests by channel count (index C - 1): host entries
+  // while planning, then one single-phase pyramid launch over a device table.
+  std::vector<kcv::PyrEntry> pyr[4];
+  kcv::PyrEntry *d_pyr[4] = {nullptr, nullptr, nullptr, nullptr};
   uint8_t *dmem = nullptr;
   size_t dmem_bytes = 0;
   FilterJob *d_jobs = nullptr;
@@ -125,12 +130,27 @@ kleidicv_error_t enqueue(kleidicv_gpu_batch_plan *p, cudaStream_t s) {
   for (size_t b = 0; b < nb && e == cudaSuccess; ++b) e = cudaStreamWaitEvent(p->branches[b], p->fork, 0);
   // Groups round-robin over the branches; the last branch also takes the
   // generic jobs and copies.
-  for (size_t g = 0; g < p->groups.size() && e == cudaSuccess; ++g) {
+  size_t lane = 0;  // next branch, round robin
+  for (size_t g = 0; g < p->groups.size() && e == cudaSuccess; ++g, ++lane) {
     const Group &gr = p->groups[g];
     BatchLaunch bl{p->d_jobs, p->d_tiles + gr.tile_off, gr.ntiles, p->d_next + g, gr.smem, gr.grid};
-    const size_t b = nb ? g % nb : 0;
+    const size_t b = nb ? lane % nb : 0;
     used[b] = true;
     e = launch_fused_batch(gr.rep, bl, ctx->d_err, nb ? p->branches[b] : s);
+  }
+  for (int c = 0; c < 4 && e == cudaSuccess; ++c) {
+    if (p->pyr[c].empty()) continue;
+    PyrLaunch L{};
+    L.entries = p->d_pyr[c];
+    L.phase_begin[0] = 0;
+    L.phase_begin[1] = static_cast<int32_t>(p->pyr[c].size());
+    L.phases = 1;
+    L.channels = c + 1;
+    L.barrier = reinterpret_cast<unsigned *>(ctx->d_err + 1);
+    L.err_flag = ctx->d_err;
+    const size_t b = nb ? lane++ % nb : 0;
+    used[b] = true;
+    e = launch_pyramid(L, ctx->sm_count, nb ? p->branches[b] : s);
   }
   cudaStream_t tail = nb ? p->branches[nb - 1] : s;
   for (size_t i = 0; i < p->generic.size() && e == cudaSuccess; ++i) {
@@ -190,6 +210,14 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
         break;
       }
       case Prepared::FUSED: {
+        if (pr.fused.mode == MODE_BLURDOWN) {
+          const FilterJob &f = pr.fused;
+          PyrEntry en;
+          pyr_entry(en, f.src, f.src_stride, f.dst, f.dst_stride, f.width, f.height, f.channels, f.border,
+                    f.border_value, 1);  // bands sized once the request count is known
+          p->pyr[f.channels - 1].push_back(en);
+          break;
+        }
         FilterJob j = pr.fused;
         // The batched kernels run fixed 4-warp CTAs over 64-row tiles with the
         // default ring (the autotune table is measured for whole-image calls).
@@ -244,10 +272,28 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
     gr.cost.clear();
   }
   p->tiles_total = all_tiles.size();
+  // Blur-and-downsample entries: bands sized for each request's share of the
+  // pyramid kernel's resident warps, items counted through the table.
+  size_t npyr_groups = 0, pyr_bytes[4] = {0, 0, 0, 0};
+  for (int c = 0; c < 4; ++c) {
+    std::vector<PyrEntry> &v = p->pyr[c];
+    if (v.empty()) continue;
+    ++npyr_groups;
+    const int share = std::max(1, pyramid_warps(c + 1, ctx->sm_count) / static_cast<int>(v.size()));
+    int32_t items = 0;
+    for (PyrEntry &en : v) {
+      pyr_entry(en, en.src, en.src_stride, en.dst, en.dst_stride, en.w, en.h, c + 1, en.border, en.border_value,
+                share);
+      items += en.item_end;
+      en.item_end = items;
+    }
+    pyr_bytes[c] = align_up(v.size() * sizeof(PyrEntry), 256);
+  }
   const size_t jobs_bytes = align_up(p->jobs.size() * sizeof(FilterJob), 256);
   const size_t tiles_bytes = align_up(all_tiles.size() * sizeof(BatchTile), 256);
   const size_t next_bytes = align_up(p->groups.size() * sizeof(int), 256);
-  p->dmem_bytes = jobs_bytes + tiles_bytes + next_bytes + generic_bytes;
+  const size_t pyr_total = pyr_bytes[0] + pyr_bytes[1] + pyr_bytes[2] + pyr_bytes[3];
+  p->dmem_bytes = jobs_bytes + tiles_bytes + next_bytes + generic_bytes + pyr_total;
   if (p->dmem_bytes) {
     p->dmem = static_cast<uint8_t *>(ctx_alloc(ctx, p->dmem_bytes));
     if (!p->dmem) {
@@ -259,11 +305,21 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
   p->d_tiles = reinterpret_cast<BatchTile *>(p->dmem + jobs_bytes);
   p->d_next = reinterpret_cast<int *>(p->dmem + jobs_bytes + tiles_bytes);
   for (size_t &off : p->generic_off) off += jobs_bytes + tiles_bytes + next_bytes;
+  {
+    size_t off = jobs_bytes + tiles_bytes + next_bytes + generic_bytes;
+    for (int c = 0; c < 4; ++c) {
+      if (!pyr_bytes[c]) continue;
+      p->d_pyr[c] = reinterpret_cast<PyrEntry *>(p->dmem + off);
+      off += pyr_bytes[c];
+    }
+  }
   // Through the pinned upload ring: no wait for the stream's earlier work.
   cudaError_t ce = upload_async(ctx, p->d_jobs, p->jobs.data(), p->jobs.size() * sizeof(FilterJob));
   if (ce == cudaSuccess)
     ce = upload_async(ctx, p->d_tiles, all_tiles.data(), all_tiles.size() * sizeof(BatchTile));
-  const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() +
+  for (int c = 0; c < 4 && ce == cudaSuccess; ++c)
+    if (p->d_pyr[c]) ce = upload_async(ctx, p->d_pyr[c], p->pyr[c].data(), p->pyr[c].size() * sizeof(PyrEntry));
+  const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() + npyr_groups +
                                           ((p->generic.empty() && p->copies.empty()) ? 0 : 1));
   if (ce == cudaSuccess) {
     // The context's branch streams and events, created once and shared.
@@ -288,7 +344,7 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
       p->joins.assign(ctx->branch_events.begin(), ctx->branch_events.begin() + nbranch);
     }
   }
-  p->kernels_per_launch = p->groups.size() + 2 * p->generic.size();
+  p->kernels_per_launch = p->groups.size() + npyr_groups + 2 * p->generic.size();
   if (ce != cudaSuccess) {
     kleidicv_gpu_batch_plan_destroy(p);
     return cuda_status(ctx, ce);

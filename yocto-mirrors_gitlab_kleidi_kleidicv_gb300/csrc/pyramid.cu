@@ -23,13 +23,15 @@
 //    registers as packed 16-bit pairs, and each destination row adds two new
 //    rows: a + e + 4 (b + d) + 6 c + 128 per lane, whose high bytes are the
 //    destination bytes.
-// Only 16-byte chunks inside the row are copied (the source must be 16-byte
-// aligned), and only destination pixels whose five source columns lie inside
-// them are stored: X in [1, (wsafe - 3) / 2] with wsafe the pixels of the
-// row's whole chunks.  The remaining pixels of each row (X = 0 and the last
-// few) are edge tasks of the same phase, scheduled first: one lane per (row,
-// element), its 25 border-mapped source bytes loaded independently.  An
-// unaligned source is edge tasks only.
+// Only aligned 16-byte blocks that lie wholly inside the row are copied.  With
+// an unaligned base or stride each staged row starts at the aligned block
+// below the strip's first byte, and the lanes shift their tap windows by that
+// row's misalignment (a funnel shift of the staged words).  Only destination
+// pixels whose five source columns lie inside the copied blocks of every row
+// are stored: X in [xl, xr] (xl = 1 for aligned rows; unaligned rows leave up
+// to 15 bytes at either end uncovered).  The remaining pixels of each row are
+// edge tasks of the same phase, scheduled first: one lane per (row, element),
+// its 25 border-mapped source bytes loaded independently.
 //
 // A pyramid is one launch: each level of each image is a phase, and phases
 // are separated by a grid-wide barrier (every CTA resident: cooperative
@@ -65,7 +67,9 @@ struct LaneGeo {
   static constexpr int OUT = B / 2;           // destination bytes of a lane
   static constexpr int NH = OUT / 2;          // packed 16-bit pairs of sums
   static constexpr int SPAN = 32 * B;         // strip bytes
-  static constexpr int CHUNKS = SPAN / 16 + 2;  // staged 16-byte chunks of a row: the strip +- 16
+  // Staged 16-byte chunks of a row: the strip +- 16 bytes, and one more for
+  // a row start up to 15 bytes past the first chunk's boundary.
+  static constexpr int CHUNKS = SPAN / 16 + 3;
   static constexpr int ROW = CHUNKS * 16;       // staged row bytes
   static constexpr int WARP_STAGE = kStageRows * ROW;
 };
@@ -154,15 +158,11 @@ __device__ bool grid_barrier(unsigned *count, unsigned epoch, int *err_flag) {
   return ok != 0;
 }
 
-// Horizontal sums of one staged source row for the lane's OUT destination
-// elements, as NH packed 16-bit pairs (sums <= 4080).  `row` is the staged
-// row, `off` the byte offset of the lane's tap window in it.
+// Horizontal sums of the lane's tap window t (NT source words) for its OUT
+// destination elements, as NH packed 16-bit pairs (sums <= 4080).
 template <int C>
-__device__ __forceinline__ void hsums(const uint8_t *row, int off, uint32_t (&hs)[LaneGeo<C>::NH]) {
+__device__ __forceinline__ void hsums_words(const uint32_t (&t)[LaneGeo<C>::NT], uint32_t (&hs)[LaneGeo<C>::NH]) {
   using G = LaneGeo<C>;
-  uint32_t t[G::NT];
-#pragma unroll
-  for (int k = 0; k < G::NT; ++k) t[k] = *reinterpret_cast<const uint32_t *>(row + off + 4 * k);
   if constexpr (C == 4) {
     // Window word k is pixel k - 2 of the lane; destination pixel m is
     // centred on pixel 2m: its taps are words 2m .. 2m + 4.
@@ -195,16 +195,55 @@ __device__ __forceinline__ void hsums(const uint8_t *row, int off, uint32_t (&hs
   }
 }
 
-// Last interior destination pixel of a level (0: none): its five source
-// columns lie inside the row's whole 16-byte chunks.
-__host__ __device__ inline int interior_last(int w, int c, bool aligned) {
-  if (!aligned) return 0;
-  const int wsafe = static_cast<int>((static_cast<long>(w) * c / 16 * 16) / c);
-  return wsafe >= 3 ? (wsafe - 3) / 2 : 0;
+// Horizontal sums of one staged source row.  `row` is the staged row, `off`
+// the byte offset of the lane's tap window in it (a multiple of 4), `mis` the
+// row's misalignment (0..15: the staged bytes start `mis` bytes before the
+// row byte that `off` counts from).
+template <int C, bool ALIGNED>
+__device__ __forceinline__ void hsums(const uint8_t *row, int off, int mis, uint32_t (&hs)[LaneGeo<C>::NH]) {
+  using G = LaneGeo<C>;
+  uint32_t t[G::NT];
+  if constexpr (ALIGNED) {
+#pragma unroll
+    for (int k = 0; k < G::NT; ++k) t[k] = *reinterpret_cast<const uint32_t *>(row + off + 4 * k);
+  } else {
+    const uint32_t *q = reinterpret_cast<const uint32_t *>(row + off + (mis & ~3));
+    const unsigned sh = 8u * static_cast<unsigned>(mis & 3);
+    uint32_t wv[G::NT + 1];
+#pragma unroll
+    for (int k = 0; k <= G::NT; ++k) wv[k] = q[k];
+#pragma unroll
+    for (int k = 0; k < G::NT; ++k) t[k] = __funnelshift_r(wv[k], wv[k + 1], sh);
+  }
+  hsums_words<C>(t, hs);
 }
 
-// One band of one strip of one entry.
-template <int C, bool FRESH>
+// Interior destination pixels of a level, [first, last] (last < first: none):
+// their five source columns lie inside the aligned 16-byte blocks wholly
+// inside every row.  Aligned rows: the blocks cover the row's first
+// 16 * floor(w c / 16) bytes.  Unaligned rows: at least bytes [15, w c - 15).
+struct Interior {
+  int first, last;
+};
+__host__ __device__ inline Interior interior(int w, int c, bool aligned) {
+  const long wc = static_cast<long>(w) * c;
+  const long covered = aligned ? wc / 16 * 16 : wc - 15;  // bytes [lead, covered) are staged
+  const int wsafe = covered > 0 ? static_cast<int>(covered / c) : 0;
+  Interior r;
+  // Leftmost tap byte 2 c (X - 1) >= lead: X >= 1 (lead 0), else X >= ceil((15 + 2c) / 2c).
+  r.first = aligned ? 1 : (14 + 4 * c) / (2 * c);
+  // Rightmost tap pixel 2 X + 2 < wsafe.
+  r.last = wsafe >= 3 ? (wsafe - 3) / 2 : -1;
+  return r;
+}
+
+__host__ __device__ inline bool rows_aligned(const uint8_t *src, int64_t stride) {
+  return ((reinterpret_cast<uintptr_t>(src) | static_cast<uintptr_t>(stride)) & 15) == 0;
+}
+
+// One band of one strip of one entry (ALIGNED: 16-byte aligned base and
+// stride).
+template <int C, bool FRESH, bool ALIGNED>
 __device__ __forceinline__ void run_band(const PyrEntry &e, uint8_t *stage, int strip, int band, int lane) {
   using G = LaneGeo<C>;
   const long wc = static_cast<long>(e.w) * C;
@@ -217,31 +256,47 @@ __device__ __forceinline__ void run_band(const PyrEntry &e, uint8_t *stage, int 
   const int Y0 = band * e.band_q + min(band, e.band_r);
   const int nrows = 2 * rows + 3;  // source rows 2 Y0 - 2 .. 2 Y1
 
-  // Copies: row rr of the stage holds source row 2 Y0 - 2 + rr; each lane
-  // copies chunks lane and lane + 32 of it, the chunks inside the row.
+  // Copies: row rr of the stage holds source row 2 Y0 - 2 + rr from row byte
+  // base - mis (mis: the row start's misalignment, 0 when aligned and for a
+  // constant-border row); each lane copies chunks lane and lane + 32 of it,
+  // the aligned blocks wholly inside the row.  The misalignments are kept as
+  // 4-bit fields for the reads.
   const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(stage));
+  uint64_t mis_lo = 0;  // rows 0 .. 15
+  uint32_t mis_hi = 0;  // rows 16 .. 18
   int rr = 0;
 #pragma unroll
   for (int grp = 0; grp < kGroups; ++grp) {
 #pragma unroll 1
     for (; rr < min(nrows, 5 * grp + 5); ++rr) {
       const int y = map_index(2 * Y0 - 2 + rr, e.h, e.border);
+      const uint8_t *srow = y < 0 ? e.src : e.src + static_cast<int64_t>(y) * e.src_stride;
+      const int mis = (ALIGNED || y < 0) ? 0 : static_cast<int>(reinterpret_cast<uintptr_t>(srow) & 15);
+      if constexpr (!ALIGNED) {
+        if (rr < 16) mis_lo |= static_cast<uint64_t>(mis) << (4 * rr);
+        else mis_hi |= static_cast<uint32_t>(mis) << (4 * (rr - 16));
+      }
 #pragma unroll
       for (int k = lane; k < G::CHUNKS; k += 32) {
-        const long x = base + 16L * k;
+        const long x = base + 16L * k - mis;
         if (y < 0) {
           *reinterpret_cast<uint4 *>(stage + rr * G::ROW + 16 * k) = make_uint4(bv4, bv4, bv4, bv4);
         } else if (x >= 0 && x + 16 <= wc) {
-          cp_async16p(sbase + rr * G::ROW + 16 * k, e.src + static_cast<int64_t>(y) * e.src_stride + x);
+          cp_async16p(sbase + rr * G::ROW + 16 * k, srow + x);
         }
       }
     }
     cp_async_commit_p();
   }
+  auto mis_of = [&](int row) -> int {
+    if constexpr (ALIGNED) return 0;
+    return row < 16 ? static_cast<int>((mis_lo >> (4 * row)) & 15) : static_cast<int>((mis_hi >> (4 * (row - 16))) & 15);
+  };
 
-  // Stored: destination elements of pixels [1, xr].
+  // Stored: destination elements of pixels [xl, xr].
+  const Interior in = interior(e.w, C, ALIGNED);
   const long oe = e0 / 2;  // first destination element of the lane
-  const long olo = C, ohi = static_cast<long>(interior_last(e.w, C, true) + 1) * C;
+  const long olo = static_cast<long>(in.first) * C, ohi = static_cast<long>(in.last + 1) * C;
   const bool stores = oe + G::OUT > olo && oe < ohi;
   const uintptr_t smask = C == 3 ? 3 : 7;
   const bool full_store =
@@ -250,17 +305,17 @@ __device__ __forceinline__ void run_band(const PyrEntry &e, uint8_t *stage, int 
 
   uint32_t a[G::NH], b[G::NH], c[G::NH];
   wait_groups(kGroups - 1);  // group 0: rows 0 .. 4
-  hsums<C>(stage, off, a);
-  hsums<C>(stage + G::ROW, off, b);
-  hsums<C>(stage + 2 * G::ROW, off, c);
+  hsums<C, ALIGNED>(stage, off, mis_of(0), a);
+  hsums<C, ALIGNED>(stage + G::ROW, off, mis_of(1), b);
+  hsums<C, ALIGNED>(stage + 2 * G::ROW, off, mis_of(2), c);
   uint8_t *drow = e.dst + static_cast<int64_t>(Y0) * e.dst_stride + oe;
 #pragma unroll 1
   for (int r = 0; r < rows; ++r) {
     // Destination row r reads stage rows 2r + 3 and 2r + 4: group (2r + 4) / 5.
     wait_groups(max(0, kGroups - 1 - (2 * r + 4) / 5));
     uint32_t d[G::NH], ee[G::NH];
-    hsums<C>(stage + (2 * r + 3) * G::ROW, off, d);
-    hsums<C>(stage + (2 * r + 4) * G::ROW, off, ee);
+    hsums<C, ALIGNED>(stage + (2 * r + 3) * G::ROW, off, mis_of(2 * r + 3), d);
+    hsums<C, ALIGNED>(stage + (2 * r + 4) * G::ROW, off, mis_of(2 * r + 4), ee);
     uint32_t s[G::NH];
 #pragma unroll
     for (int k = 0; k < G::NH; ++k) s[k] = a[k] + ee[k] + 0x00800080u + 4u * (b[k] + d[k]) + 6u * c[k];
@@ -298,18 +353,30 @@ __device__ __forceinline__ void run_band(const PyrEntry &e, uint8_t *stage, int 
   __syncwarp();
 }
 
-// Edge task `task` of entry e: destination element (Y, X, ch) for the edge
-// pixels X = 0 and X in [max(1, xr + 1), ow).
+// Edge pixels of a row: X in [0, xl) and [xs, ow), with xl = min(first, ow)
+// and xs = max(last + 1, xl).
+struct EdgeSplit {
+  int xl, xs, per_row;  // per_row: edge elements of a destination row
+};
+__host__ __device__ inline EdgeSplit edge_split(int w, int ow, int c, bool aligned) {
+  const Interior in = interior(w, c, aligned);
+  EdgeSplit s;
+  s.xl = in.first < ow ? in.first : ow;
+  s.xs = in.last + 1 > s.xl ? in.last + 1 : s.xl;
+  s.per_row = c * (s.xl + (ow > s.xs ? ow - s.xs : 0));
+  return s;
+}
+
+// Edge task `task` of entry e: destination element (Y, X, ch) of an edge
+// pixel.
 template <int C, bool FRESH>
 __device__ __forceinline__ void edge_task(const PyrEntry &e, int task) {
-  const bool aligned = ((reinterpret_cast<uintptr_t>(e.src) | static_cast<uintptr_t>(e.src_stride)) & 15) == 0;
-  const int xr = interior_last(e.w, C, aligned);
-  const int xs = xr + 1 > 1 ? xr + 1 : 1;  // first right-edge pixel
-  const int per_row = C * (1 + (e.ow > xs ? e.ow - xs : 0));
+  const EdgeSplit sp = edge_split(e.w, e.ow, C, rows_aligned(e.src, e.src_stride));
+  const int per_row = sp.per_row;
   if (task >= per_row * e.oh) return;
   const int Y = task / per_row, q = task - Y * per_row;
   const int p = q / C, ch = q - p * C;
-  const int X = p == 0 ? 0 : xs + p - 1;
+  const int X = p < sp.xl ? p : sp.xs + p - sp.xl;
   const uint32_t bv = static_cast<uint32_t>(e.border_value) & 0xFFu;
   const uint8_t *rows[5];
   long cols[5];
@@ -344,7 +411,11 @@ __device__ __forceinline__ void run_item(const PyrEntry &en, uint8_t *stage, int
     // strips at the row's ends.
     const int m = local - en.edge_items;
     const int band = m / en.strips, q = m - band * en.strips;
-    run_band<C, FRESH>(en, stage, static_cast<int>((q + 7L * band) % en.strips), band, lane);
+    const int strip = static_cast<int>((q + 7L * band) % en.strips);
+    if (rows_aligned(en.src, en.src_stride))
+      run_band<C, FRESH, true>(en, stage, strip, band, lane);
+    else
+      run_band<C, FRESH, false>(en, stage, strip, band, lane);
   }
 }
 
@@ -470,11 +541,13 @@ void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst
   e.h = h;
   e.ow = (w + 1) / 2;
   e.oh = (h + 1) / 2;
-  const bool aligned = ((reinterpret_cast<uintptr_t>(src) | static_cast<uintptr_t>(src_stride)) & 15) == 0;
-  // A strip makes 32 lanes x (8, or 12 for three channels) destination bytes.
+  const bool aligned = rows_aligned(src, src_stride);
+  const EdgeSplit sp = edge_split(w, e.ow, channels, aligned);
+  // A strip makes 32 lanes x (8, or 12 for three channels) destination bytes;
+  // no strips when no pixel is interior.
   const long strip_out = 32L * (channels == 3 ? 12 : 8);
   const long owc = static_cast<long>(e.ow) * channels;
-  e.strips = aligned ? static_cast<int32_t>((owc + strip_out - 1) / strip_out) : 0;
+  e.strips = sp.xs > sp.xl ? static_cast<int32_t>((owc + strip_out - 1) / strip_out) : 0;
   // Bands of at most kPyrBandRows rows, as many as give every warp the same
   // number of items.
   long bands = 0;
@@ -487,11 +560,7 @@ void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst
   e.bands = static_cast<int32_t>(bands);
   e.band_q = bands > 0 ? static_cast<int32_t>(e.oh / bands) : 0;
   e.band_r = bands > 0 ? static_cast<int32_t>(e.oh % bands) : 0;
-  // Edge pixels per destination row: X = 0 and X >= max(1, xr + 1).
-  const int xr = interior_last(w, channels, aligned);
-  const int xs = xr + 1 > 1 ? xr + 1 : 1;
-  const long per_row = static_cast<long>(channels) * (1 + (e.ow > xs ? e.ow - xs : 0));
-  e.edge_items = static_cast<int32_t>((per_row * e.oh + 31) / 32);
+  e.edge_items = static_cast<int32_t>((static_cast<long>(sp.per_row) * e.oh + 31) / 32);
   e.item_end = e.edge_items + static_cast<int32_t>(e.strips * bands);
 }
 
