@@ -32,6 +32,7 @@
 #include <algorithm>
 
 #include "launch.h"
+#include "resident.cuh"
 #include "sepfused.cuh"
 
 namespace kcv {
@@ -295,12 +296,10 @@ __global__ void __launch_bounds__(kThreadsG, K == 7 ? 4 : 5) gauss8_kernel(const
 template <int K>
 cudaError_t launch8(Gauss8Job &j, int sm_count, cudaStream_t stream) {
   auto kern = gauss8_kernel<K>;
-  const cudaError_t ea = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemG);
-  if (ea != cudaSuccess) return ea;
   int occ = 0;
-  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreadsG, kSmemG);
+  const cudaError_t err = resident_ctas_per_sm<gauss8_kernel<K>>(kThreadsG, kSmemG, &occ);
   if (err != cudaSuccess) return err;
-  const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
+  const long resident = static_cast<long>(occ) * std::max(sm_count, 1);
   const long slots = resident * kWarpsG;
   j.strips = (j.w + kStripPix - 1) / kStripPix;
   // Bands of at most kGauss8MaxBand rows, as many as give every resident warp

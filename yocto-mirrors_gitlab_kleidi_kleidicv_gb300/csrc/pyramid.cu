@@ -44,6 +44,7 @@
 #include <algorithm>
 
 #include "launch.h"
+#include "resident.cuh"
 #include "sepfused.cuh"
 
 namespace kcv {
@@ -462,12 +463,9 @@ __global__ void __launch_bounds__(kThreads) pyramid_kernel(const __grid_constant
 
 template <int C>
 int warps_c(int sm_count) {
-  auto kern = pyramid_kernel<C>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes<C>()) != cudaSuccess)
-    return 0;
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, smem_bytes<C>()) != cudaSuccess) return 0;
-  return std::max(occ, 1) * std::max(sm_count, 1) * kWarps;
+  if (resident_ctas_per_sm<pyramid_kernel<C>>(kThreads, smem_bytes<C>(), &occ) != cudaSuccess) return 0;
+  return occ * std::max(sm_count, 1) * kWarps;
 }
 
 template <int C>

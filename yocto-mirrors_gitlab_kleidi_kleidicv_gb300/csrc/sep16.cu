@@ -47,6 +47,7 @@
 #include <cstdlib>
 
 #include "launch.h"
+#include "resident.cuh"
 #include "sepfused.cuh"
 
 namespace kcv {
@@ -335,12 +336,10 @@ __global__ void __launch_bounds__(kThreads16, 5) sep16_kernel(const __grid_const
 template <bool S16>
 cudaError_t launch16(Sep16Job &j, int sm_count, cudaStream_t stream) {
   auto kern = sep16_kernel<S16>;
-  const cudaError_t ea = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem16);
-  if (ea != cudaSuccess) return ea;
   int occ = 0;
-  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads16, kSmem16);
+  const cudaError_t err = resident_ctas_per_sm<sep16_kernel<S16>>(kThreads16, kSmem16, &occ);
   if (err != cudaSuccess) return err;
-  const long resident = static_cast<long>(std::max(occ, 1)) * std::max(sm_count, 1);
+  const long resident = static_cast<long>(occ) * std::max(sm_count, 1);
   const long slots = resident * kWarps16;
   j.strips = (j.w + kStripElems - 1) / kStripElems;
   // Bands of at most kSep16MaxBand rows, as many as give every resident warp
