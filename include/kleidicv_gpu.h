@@ -33,6 +33,8 @@
  *  kleidicv_gpu_sobel_3x3_vertical_s16_u8
  *                                        kleidicv/include/kleidicv/kleidicv.h:2006-2008
  *                                        (kleidicv/src/filters/sobel_api.cpp:53-58)
+ *  kleidicv_gpu_<each of the six above>_sme
+ *                                        kleidicv/include/kleidicv/kleidicv.h:2010,2054,2097,2109,2165,2220
  *  kleidicv_gpu_median_blur_{s8,u8,u16,s16,u32,s32,f32}
  *                                        kleidicv/include/kleidicv/kleidicv.h:2225-2302
  *                                        (kleidicv/src/filters/median_blur_api.cpp:42-242)
@@ -156,6 +158,36 @@ kleidicv_error_t kleidicv_gpu_sobel_3x3_horizontal_s16_u8(
     size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
 
 kleidicv_error_t kleidicv_gpu_sobel_3x3_vertical_s16_u8(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
+
+/* The `_sme` twins (kleidicv.h:2010, 2054, 2097, 2109, 2165, 2220): in KleidiCV
+ * the suffix selects the CPU backend and changes neither semantics nor the
+ * parameter contract (kleidicv.h:23-35); here each twin is the same call as
+ * its base entry. */
+kleidicv_error_t kleidicv_gpu_gaussian_blur_u8_sme(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, size_t kernel_width,
+    size_t kernel_height, float sigma_x, float sigma_y,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u8_sme(
+    const uint8_t *src, size_t src_stride, uint8_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint8_t *kernel_x,
+    size_t kernel_width, const uint8_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_separable_filter_2d_u16_sme(
+    const uint16_t *src, size_t src_stride, uint16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, const uint16_t *kernel_x,
+    size_t kernel_width, const uint16_t *kernel_y, size_t kernel_height,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_blur_and_downsample_u8_sme(
+    const uint8_t *src, size_t src_stride, size_t src_width, size_t src_height,
+    uint8_t *dst, size_t dst_stride, size_t channels,
+    kleidicv_border_type_t border_type, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_sobel_3x3_horizontal_s16_u8_sme(
+    const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
+    size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
+kleidicv_error_t kleidicv_gpu_sobel_3x3_vertical_s16_u8_sme(
     const uint8_t *src, size_t src_stride, int16_t *dst, size_t dst_stride,
     size_t width, size_t height, size_t channels, kleidicv_gpu_context_t *ctx);
 

@@ -160,6 +160,12 @@ SIGNATURES = {
     "kleidicv_gpu_gaussian_blur_u8_noalloc": (_i, [_vp, _sz, _vp, _sz, _sz, _sz, _sz, _sz, _sz, _f, _f,
                                                    _i, _vp]),
 }
+# The `_sme` twins take the argument lists of their base entries.
+SME_TWINS = ("kleidicv_gpu_gaussian_blur_u8", "kleidicv_gpu_separable_filter_2d_u8",
+             "kleidicv_gpu_separable_filter_2d_u16", "kleidicv_gpu_blur_and_downsample_u8",
+             "kleidicv_gpu_sobel_3x3_horizontal_s16_u8", "kleidicv_gpu_sobel_3x3_vertical_s16_u8")
+for _name in SME_TWINS:
+    SIGNATURES[_name + "_sme"] = SIGNATURES[_name]
 
 _lib = None
 
