@@ -68,10 +68,13 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="c1,batched,pyramid,lk_pyramid,sobel,median,thread_api,serving",
                     help="extra measurements added to the line (comma list, or 'none')")
-    ap.add_argument("--profile-op", choices=("gauss", "u16", "s16", "blurdown", "sobel"), default=None,
+    ap.add_argument("--profile-op", choices=("gauss", "u16", "s16", "blurdown", "sobel", "arbitrary", "median5",
+                                             "median15", "lk"), default=None,
                     help="run one workload 3 times on cuda:0 and exit (a small command for profiler captures): "
                          "the sweep's Gaussian / u16 REFLECT / s16 REFLECT call, blur_and_downsample_u8 of a "
-                         "4096x4096x1 image, or the d/dx Sobel of a 3840x2160x1 image")
+                         "4096x4096x1 image, the d/dx Sobel of a 3840x2160x1 image, a 31x31 sigma 5 Gaussian "
+                         "(REPLICATE, the generic two-pass kernel) of a 3840x2160x1 image, the 5x5 / 15x15 u8 "
+                         "median of a 1920x1080x1 image, or the 4-level LK pyramid of a 1920x1080x1 image")
     ap.add_argument("--profile-range", type=int, default=0,
                     help="with --profile-op: N calls over rotating buffer sets larger than twice the L2, between "
                          "cudaProfilerStart and cudaProfilerStop (an ncu --replay-mode range window that also "
@@ -1289,6 +1292,12 @@ def profile_op(name, range_calls=0):
     elif name == "blurdown":
         host = _pyr_image(rng, 4096, 4096, 1)
         out_shape, out_dtype = (2048, 2048), torch.uint8
+    elif name == "arbitrary":
+        host = rng.integers(0, 256, (H, W), dtype=np.uint8)
+        out_shape, out_dtype = (H, W), torch.uint8
+    elif name in ("median5", "median15", "lk"):
+        host = rng.integers(0, 256, (1080, 1920), dtype=np.uint8)
+        out_shape, out_dtype = (1080, 1920), torch.uint8
     else:
         host = rng.integers(0, 256, (H, W), dtype=np.uint8)
         out_shape, out_dtype = (H, W), torch.int16
@@ -1309,6 +1318,19 @@ def profile_op(name, range_calls=0):
         if name == "blurdown":
             return kcv.blur_and_downsample_u8(src.data_ptr(), 4096, 4096, 4096, dst.data_ptr(), 2048, 1,
                                               kcv.REVERSE, ctx)
+        if name == "arbitrary":
+            return kcv.gaussian_blur_u8(src.data_ptr(), W, dst.data_ptr(), W, W, H, 1, 31, 31, 5.0, 5.0,
+                                        kcv.REPLICATE, ctx)
+        if name in ("median5", "median15"):
+            k = 5 if name == "median5" else 15
+            return kcv.median_blur("u8", src.data_ptr(), 1920, dst.data_ptr(), 1920, 1920, 1080, 1, k, k,
+                                   kcv.REPLICATE, ctx)
+        if name == "lk":
+            pyr = kcv.LKPyramid(src.data_ptr(), 1920, 1920, 1080, 1, 4, 21, 21, ctx)
+            err = pyr.error
+            if err == kcv.OK:
+                pyr.close()
+            return err
         return kcv.sobel_3x3_horizontal_s16_u8(src.data_ptr(), W, dst.data_ptr(), 2 * W, W, H, 1, ctx)
 
     n = 3 if not range_calls else 1

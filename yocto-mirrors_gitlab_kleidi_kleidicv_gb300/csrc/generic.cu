@@ -32,26 +32,66 @@ __device__ __forceinline__ uint32_t weight(const GenericJob &j, int t) {
   return j.half[t <= r ? t : j.ksize - 1 - t];
 }
 
-constexpr int kRowsPerThread = 16;
+// Destination rows per thread in pass 1: few enough that a 4K image fills
+// the GPU more than once (16 rows gave 0.44 waves on 3840x2160x1).
+constexpr int kRowsPerThread = 4;
 constexpr int kHThreads = 256;
 constexpr int kHElems = 4 * kHThreads;  // row elements per CTA in pass 2
 
+// The full kernel's weights (ksize <= 255) into shared memory, once per CTA:
+// the tap loops then read them without the mirror select.
+__device__ __forceinline__ void stage_weights(const GenericJob &j, uint32_t *wts) {
+  for (int t = threadIdx.x; t < j.ksize; t += blockDim.x) wts[t] = weight(j, t);
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(256) generic_vertical(const __grid_constant__ GenericJob j,
                                                         uint8_t *vbuf, size_t vstride) {
+  __shared__ uint32_t wts[256];
+  stage_weights(j, wts);
   const long wc = static_cast<long>(j.width) * j.channels;
   const long x = (static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
   if (x >= wc) return;
   const int ne = static_cast<int>(wc - x < 4 ? wc - x : 4);
   const int r = j.ksize / 2;
+  // Whole 4-byte words when the column's words are 4-byte aligned in every
+  // row.
+  const bool words = ne == 4 && ((reinterpret_cast<uintptr_t>(j.src + x) | static_cast<uintptr_t>(j.src_stride)) & 3) == 0;
   // Row blocks loop over the grid's y extent, which the hardware caps at 65535.
   for (long yb = blockIdx.y; yb * kRowsPerThread < j.height; yb += gridDim.y) {
     const int y0 = static_cast<int>(yb * kRowsPerThread);
     const int y1 = min(y0 + kRowsPerThread, j.height);
+    if (words && y0 >= r && y1 - 1 + r < j.height) {
+      // Every tap row inside the image: step a row pointer, no border map.
+      for (int y = y0; y < y1; ++y) {
+        uint32_t acc[4] = {0, 0, 0, 0};
+        const uint8_t *row = j.src + static_cast<int64_t>(y - r) * j.src_stride + x;
+        for (int t = 0; t < j.ksize; ++t, row += j.src_stride) {
+          const uint32_t g = wts[t];
+          const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(row));
+          acc[0] += g * (w & 0xFFu);
+          acc[1] += g * ((w >> 8) & 0xFFu);
+          acc[2] += g * ((w >> 16) & 0xFFu);
+          acc[3] += g * (w >> 24);
+        }
+        uint32_t o = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          o |= (j.vert_saturates ? round_sat(acc[e]) : round_wrap(acc[e])) << (8 * e);
+        uint8_t *out = vbuf + static_cast<int64_t>(y) * vstride + x;
+        if ((reinterpret_cast<uintptr_t>(out) & 3) == 0) {
+          *reinterpret_cast<uint32_t *>(out) = o;
+        } else {
+          for (int e = 0; e < 4; ++e) out[e] = static_cast<uint8_t>(o >> (8 * e));
+        }
+      }
+      continue;
+    }
     for (int y = y0; y < y1; ++y) {
       uint32_t acc[4] = {0, 0, 0, 0};
       for (int t = 0; t < j.ksize; ++t) {
         const int ry = map_index(y + t - r, j.height, j.border);
-        const uint32_t g = weight(j, t);
+        const uint32_t g = wts[t];
         if (ry < 0) {
           const uint32_t bv = static_cast<uint32_t>(j.border_value) & 0xFFu;
           for (int e = 0; e < 4; ++e) acc[e] += g * bv;
@@ -105,6 +145,8 @@ __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_con
                                                                 const uint8_t *vbuf,
                                                                 size_t vstride) {
   extern __shared__ uint8_t seg[];
+  __shared__ uint32_t wts[256];
+  stage_weights(j, wts);
   const int c = j.channels;
   const int r = j.ksize / 2;
   const long wc = static_cast<long>(j.width) * c;
@@ -137,7 +179,7 @@ __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_con
       const long x = x0 + local;
       if (x >= wc) break;
       uint32_t acc = 0;
-      for (int t = 0; t < j.ksize; ++t) acc += weight(j, t) * seg[local + t * c];
+      for (int t = 0; t < j.ksize; ++t) acc += wts[t] * seg[local + t * c];
       if (right_quirk && x >= wc - j.arb_border_len) {
         const uint8_t *last = vrow + wc - c;
         for (int d = 1; d <= r; ++d) {
