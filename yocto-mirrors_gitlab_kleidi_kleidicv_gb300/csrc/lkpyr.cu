@@ -5,8 +5,9 @@
 // Every level is an image with a reflect-101 border of (window_width,
 // window_height) pixels and the interleaved (dx, dy) Scharr derivatives of
 // that image (s16, 2 x channels per pixel) with a zero halo of the same size.
-// Level l >= 1 is blur_and_downsample (REVERSE) of level l - 1 by the fused
-// stencil, written straight into the level's interior; one "finish" kernel per
+// Level l >= 1 is blur_and_downsample (REVERSE) of level l - 1 through the
+// blur-and-downsample call path (the pyramid kernel), written straight into
+// the level's interior; one "finish" kernel per
 // level then writes the border (and, for level 0, the interior copy) and the
 // Scharr derivatives, reading the interior with the reflect-101 index map
 // instead of waiting for the border to exist.
