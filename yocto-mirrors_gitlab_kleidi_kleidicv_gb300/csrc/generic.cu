@@ -144,7 +144,9 @@ __device__ __forceinline__ int right_lane_channel(long e, int d, int c, long wc,
 __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_constant__ GenericJob j,
                                                                 const uint8_t *vbuf,
                                                                 size_t vstride) {
-  extern __shared__ uint8_t seg[];
+  // seg holds row elements [x0 - halo, x0 + kHElems + halo) of the
+  // intermediate, element x0 at the 4-aligned byte `lead`.
+  extern __shared__ __align__(16) uint8_t seg_mem[];
   __shared__ uint32_t wts[256];
   stage_weights(j, wts);
   const int c = j.channels;
@@ -152,15 +154,27 @@ __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_con
   const long wc = static_cast<long>(j.width) * c;
   const long x0 = static_cast<long>(blockIdx.x) * kHElems;
   const int halo = r * c;
-  const int seg_len = kHElems + 2 * halo;
+  const int lead = (halo + 3) & ~3;
+  uint8_t *seg = seg_mem + (lead - halo);  // seg[i]: element x0 - halo + i
+  const uint32_t *seg32 = reinterpret_cast<const uint32_t *>(seg_mem);
+  const int n = static_cast<int>(wc - x0 < kHElems ? wc - x0 : kHElems);  // interior elements
+  const bool words = ((reinterpret_cast<uintptr_t>(vbuf) | static_cast<uintptr_t>(vstride)) & 3) == 0;
   const bool right_quirk = j.arbitrary && c > 1 && x0 + kHElems > wc - j.arb_border_len;
+  const int local0 = threadIdx.x * 4;  // the thread's first element of the segment
+  const int ne = static_cast<int>(n - local0 < 4 ? n - local0 : 4);
   // Rows loop over the grid's y extent, which the hardware caps at 65535.
   for (int y = blockIdx.y; y < j.height; y += gridDim.y) {
     const uint8_t *vrow = vbuf + static_cast<int64_t>(y) * vstride;
     __syncthreads();  // the previous row's reads of seg are done
-    // Stage [x0 - halo, x0 + kHElems + halo) with the border resolved per element.
-    for (int i = threadIdx.x; i < seg_len; i += blockDim.x) {
-      const long xe = x0 - halo + i;
+    // The interior as words where the rows allow, the rest byte by byte.
+    const int nw = words ? n / 4 : 0;
+    for (int q = threadIdx.x; q < nw; q += blockDim.x)
+      reinterpret_cast<uint32_t *>(seg_mem + lead)[q] = reinterpret_cast<const uint32_t *>(vrow + x0)[q];
+    for (int i = 4 * nw + threadIdx.x; i < n; i += blockDim.x) seg[halo + i] = vrow[x0 + i];
+    // The halos, with the border resolved per element.
+    for (int i = threadIdx.x; i < 2 * halo; i += blockDim.x) {
+      const int idx = i < halo ? i : n + i;  // [0, halo) and [halo + n, 2 halo + n)
+      const long xe = x0 - halo + idx;
       uint8_t v;
       if (xe >= 0 && xe < wc) {
         v = vrow[xe];
@@ -170,24 +184,35 @@ __global__ void __launch_bounds__(kHThreads) generic_horizontal(const __grid_con
         const int mc = map_index(static_cast<int>(col), j.width, j.border);
         v = mc < 0 ? static_cast<uint8_t>(j.v_const) : vrow[static_cast<long>(mc) * c + ch];
       }
-      seg[i] = v;
+      seg[idx] = v;
     }
     __syncthreads();
+    if (ne <= 0) continue;
+    // Tap t of the thread's 4 elements: the 4 bytes at segment position
+    // local0 + t c, from the two words around them.
+    uint32_t acc[4] = {0, 0, 0, 0};
+    int p = (lead - halo) + local0;  // byte of tap 0, element 0
+    for (int t = 0; t < j.ksize; ++t, p += c) {
+      const uint32_t g = wts[t];
+      const uint32_t v = __funnelshift_r(seg32[p >> 2], seg32[(p >> 2) + 1], 8 * (p & 3));
+      acc[0] += g * (v & 0xFFu);
+      acc[1] += g * ((v >> 8) & 0xFFu);
+      acc[2] += g * ((v >> 16) & 0xFFu);
+      acc[3] += g * (v >> 24);
+    }
     uint8_t *drow = j.dst + static_cast<int64_t>(y) * j.dst_stride;
-    for (int k = 0; k < 4; ++k) {
-      const int local = threadIdx.x * 4 + k;
+    for (int k = 0; k < ne; ++k) {
+      const int local = local0 + k;
       const long x = x0 + local;
-      if (x >= wc) break;
-      uint32_t acc = 0;
-      for (int t = 0; t < j.ksize; ++t) acc += wts[t] * seg[local + t * c];
+      uint32_t a = acc[k];
       if (right_quirk && x >= wc - j.arb_border_len) {
         const uint8_t *last = vrow + wc - c;
         for (int d = 1; d <= r; ++d) {
           const int qc = right_lane_channel(x, d, c, wc, j.arb_border_len);
-          if (qc >= 0) acc = acc - weight(j, r + d) * seg[local + (r + d) * c] + weight(j, r + d) * last[qc];
+          if (qc >= 0) a = a - wts[r + d] * seg[local + (r + d) * c] + wts[r + d] * last[qc];
         }
       }
-      drow[x] = static_cast<uint8_t>(h_saturates(j, x, wc) ? round_sat(acc) : round_wrap(acc));
+      drow[x] = static_cast<uint8_t>(h_saturates(j, x, wc) ? round_sat(a) : round_wrap(a));
     }
   }
 }
@@ -203,7 +228,10 @@ cudaError_t launch_generic_gaussian(const GenericJob &job, uint8_t *scratch, siz
   generic_vertical<<<g1, 256, 0, stream>>>(job, scratch, scratch_stride);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const size_t smem = kHElems + 2 * static_cast<size_t>(job.ksize / 2) * job.channels;
+  // The segment (halos on either side, the interior from a 4-aligned byte)
+  // and 8 bytes that the last taps' word reads may touch.
+  const size_t halo = static_cast<size_t>(job.ksize / 2) * job.channels;
+  const size_t smem = ((halo + 3) & ~static_cast<size_t>(3)) + kHElems + halo + 8;
   dim3 g2(static_cast<unsigned>((wc + kHElems - 1) / kHElems),
           static_cast<unsigned>(job.height < 65535 ? job.height : 65535));
   generic_horizontal<<<g2, kHThreads, smem, stream>>>(job, scratch, scratch_stride);
