@@ -16,7 +16,11 @@
 //    both passes is an integer of magnitude <= 2^24, held exactly, and no
 //    saturating s32 add of the reference can trigger.
 // Both passes run on element pairs with the paired fp32 operations of sm_100+
-// (__ffma2_rn: per component the same rounding as fmaf).  Conversions avoid
+// (__ffma2_rn: per component the same rounding as fmaf).  A lane's 8
+// elements pair as (j, j + 4), so that a horizontal tap at distance d of
+// pair j is the lane's own pair j + d wherever that lies in the lane; only
+// the four pairs reaching into the neighbour lanes are assembled (one
+// shuffle each).  Conversions avoid
 // the slow integer<->float units: a 16-bit value v becomes
 // the float 2^23 + v by placing its bits under the exponent of 2^23 (s16 is
 // first biased by 2^15 with an xor), and a result r in [0, 65535] (u16, the
@@ -74,25 +78,31 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Element pairs: x[i] = elements (2i, 2i + 1) of the lane.
+// Element pairs: x[j] = elements (j, j + 4) of the lane, so that the
+// horizontal taps of a pair at distance d are the pair j + d whenever it lies
+// in the lane (0 <= j + d <= 3).
 template <bool S16>
 __device__ __forceinline__ void to_float2(const uint4 &raw, float2 (&x)[kLaneElems / 2]) {
   constexpr float bias = S16 ? 8421376.0f : 8388608.0f;  // 2^23 (+ 2^15)
-  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};
+  const uint32_t w[4] = {raw.x, raw.y, raw.z, raw.w};  // w[i]: elements (2i, 2i + 1)
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t v = S16 ? (w[i] ^ 0x80008000u) : w[i];
-    const float2 f = make_float2(__uint_as_float(__byte_perm(v, 0x4B000000u, 0x7410)),
-                                 __uint_as_float(__byte_perm(v, 0x4B000000u, 0x7432)));
-    x[i] = __fadd2_rn(f, make_float2(-bias, -bias));
+  for (int i = 0; i < 2; ++i) {
+    const uint32_t a = S16 ? (w[i] ^ 0x80008000u) : w[i];          // elements 2i, 2i + 1
+    const uint32_t b = S16 ? (w[i + 2] ^ 0x80008000u) : w[i + 2];  // elements 2i + 4, 2i + 5
+    const float2 lo = make_float2(__uint_as_float(__byte_perm(a, 0x4B000000u, 0x7410)),
+                                  __uint_as_float(__byte_perm(b, 0x4B000000u, 0x7410)));
+    const float2 hi = make_float2(__uint_as_float(__byte_perm(a, 0x4B000000u, 0x7432)),
+                                  __uint_as_float(__byte_perm(b, 0x4B000000u, 0x7432)));
+    x[2 * i] = __fadd2_rn(lo, make_float2(-bias, -bias));
+    x[2 * i + 1] = __fadd2_rn(hi, make_float2(-bias, -bias));
   }
 }
 
 // Horizontal pass of one element pair from its tap pairs (the taps of both
-// elements, pair by pair); returns the two result words (each a float whose
-// low 16 bits are the result) packed as two 16-bit values.
+// elements, pair by pair); returns the two result words, each a float whose
+// low 16 bits are the result.
 template <bool S16>
-__device__ __forceinline__ uint32_t hfinish2(const float2 (&kx)[5], float2 a, float2 b, float2 c, float2 d,
+__device__ __forceinline__ uint2 hfinish2(const float2 (&kx)[5], float2 a, float2 b, float2 c, float2 d,
                                              float2 e) {
   if constexpr (S16) {
     float2 acc = __fmul2_rn(kx[0], a);
@@ -103,7 +113,7 @@ __device__ __forceinline__ uint32_t hfinish2(const float2 (&kx)[5], float2 a, fl
     acc.x = fminf(fmaxf(acc.x, -32768.0f), 32767.0f);
     acc.y = fminf(fmaxf(acc.y, -32768.0f), 32767.0f);
     acc = __fadd2_rn(acc, make_float2(12582912.0f, 12582912.0f));  // 1.5 * 2^23 + r
-    return __byte_perm(__float_as_uint(acc.x), __float_as_uint(acc.y), 0x5410);
+    return make_uint2(__float_as_uint(acc.x), __float_as_uint(acc.y));
   } else {
     float2 acc = __ffma2_rn(kx[0], a, make_float2(8388608.0f, 8388608.0f));  // 2^23 + sum
     acc = __ffma2_rn(kx[1], b, acc);
@@ -111,8 +121,7 @@ __device__ __forceinline__ uint32_t hfinish2(const float2 (&kx)[5], float2 a, fl
     acc = __ffma2_rn(kx[3], d, acc);
     acc = __ffma2_rn(kx[4], e, acc);
     // 2^23 + min(sum, 65535)
-    return __byte_perm(__float_as_uint(fminf(acc.x, 8454143.0f)), __float_as_uint(fminf(acc.y, 8454143.0f)),
-                       0x5410);
+    return make_uint2(__float_as_uint(fminf(acc.x, 8454143.0f)), __float_as_uint(fminf(acc.y, 8454143.0f)));
   }
 }
 
@@ -121,27 +130,29 @@ __device__ __forceinline__ uint32_t hfinish2(const float2 (&kx)[5], float2 a, fl
 template <bool S16, int S0>
 __device__ __forceinline__ uint4 filter_row(const float2 (&win)[5][kLaneElems / 2], const float2 (&kx)[5],
                                             const float2 (&ky)[5]) {
-  // P[q]: vertical sums of elements (2q - 2, 2q - 1) of the lane; P[0] and
-  // P[5] come from the neighbour lanes.
-  float2 P[6];
+  // V[j]: vertical sums of elements (j, j + 4) of the lane.
+  float2 V[4];
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
     float2 acc = __fmul2_rn(ky[0], win[S0 % 5][m]);
     acc = __ffma2_rn(ky[1], win[(S0 + 1) % 5][m], acc);
     acc = __ffma2_rn(ky[2], win[(S0 + 2) % 5][m], acc);
     acc = __ffma2_rn(ky[3], win[(S0 + 3) % 5][m], acc);
-    P[m + 1] = __ffma2_rn(ky[4], win[(S0 + 4) % 5][m], acc);
+    V[m] = __ffma2_rn(ky[4], win[(S0 + 4) % 5][m], acc);
   }
-  P[0] = make_float2(__shfl_up_sync(0xffffffffu, P[4].x, 1), __shfl_up_sync(0xffffffffu, P[4].y, 1));
-  P[5] = make_float2(__shfl_down_sync(0xffffffffu, P[1].x, 1), __shfl_down_sync(0xffffffffu, P[1].y, 1));
-  // Odd taps read the pairs shifted by one element.
-  float2 Q[5];
-#pragma unroll
-  for (int q = 0; q < 5; ++q) Q[q] = make_float2(P[q].y, P[q + 1].x);
-  uint32_t o[4];
-#pragma unroll
-  for (int m = 0; m < 4; ++m) o[m] = hfinish2<S16>(kx, P[m], Q[m], P[m + 1], Q[m + 1], P[m + 2]);
-  return make_uint4(o[0], o[1], o[2], o[3]);
+  // The pairs at j + d = -2, -1 (elements -2, -1 are the left lane's 6, 7)
+  // and j + d = 4, 5 (elements 8, 9 are the right lane's 0, 1).
+  const float2 Cm2 = make_float2(__shfl_up_sync(0xffffffffu, V[2].y, 1), V[2].x);
+  const float2 Cm1 = make_float2(__shfl_up_sync(0xffffffffu, V[3].y, 1), V[3].x);
+  const float2 C4 = make_float2(V[0].y, __shfl_down_sync(0xffffffffu, V[0].x, 1));
+  const float2 C5 = make_float2(V[1].y, __shfl_down_sync(0xffffffffu, V[1].x, 1));
+  const uint2 h0 = hfinish2<S16>(kx, Cm2, Cm1, V[0], V[1], V[2]);
+  const uint2 h1 = hfinish2<S16>(kx, Cm1, V[0], V[1], V[2], V[3]);
+  const uint2 h2 = hfinish2<S16>(kx, V[0], V[1], V[2], V[3], C4);
+  const uint2 h3 = hfinish2<S16>(kx, V[1], V[2], V[3], C4, C5);
+  // Result j sits in the low 16 bits of h_j.x, result j + 4 in those of h_j.y.
+  return make_uint4(__byte_perm(h0.x, h1.x, 0x5410), __byte_perm(h2.x, h3.x, 0x5410),
+                    __byte_perm(h0.y, h1.y, 0x5410), __byte_perm(h2.y, h3.y, 0x5410));
 }
 
 __host__ __device__ inline int full_span(int w) { return w / kLaneElems * kLaneElems; }
@@ -192,9 +203,13 @@ __device__ __forceinline__ void edge_element16(const Sep16Job &j, int y, int x) 
   }
   // The pair form with the element in both halves.
   const uint32_t bits = hfinish2<S16>(kx, make_float2(V[0], V[0]), make_float2(V[1], V[1]), make_float2(V[2], V[2]),
-                                      make_float2(V[3], V[3]), make_float2(V[4], V[4]));
+                                      make_float2(V[3], V[3]), make_float2(V[4], V[4])).x;
   reinterpret_cast<uint16_t *>(j.dst + static_cast<int64_t>(y) * j.dst_stride)[x] = static_cast<uint16_t>(bits);
 }
+
+template <bool S16, bool SIMPLE>
+__device__ __forceinline__ void band_loop16(const Sep16Job &j, const uint4 *stage, int lane, int rows, uint8_t *d,
+                                            long e0, int wf, bool outputs, bool full_store);
 
 template <bool S16>
 __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int strip, int band, int lane) {
@@ -267,6 +282,17 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
     }
   }
 
+  uint8_t *d = j.dst + static_cast<int64_t>(y0) * j.dst_stride + 2 * e0;
+  // The byte-store path only where some lane of the warp needs it.
+  if (__all_sync(0xffffffffu, !outputs || full_store))
+    band_loop16<S16, true>(j, stage, lane, rows, d, e0, wf, outputs, full_store);
+  else
+    band_loop16<S16, false>(j, stage, lane, rows, d, e0, wf, outputs, full_store);
+}
+
+template <bool S16, bool SIMPLE>
+__device__ __forceinline__ void band_loop16(const Sep16Job &j, const uint4 *stage, int lane, int rows, uint8_t *d,
+                                            long e0, int wf, bool outputs, bool full_store) {
   float2 kx[5], ky[5];
 #pragma unroll
   for (int t = 0; t < 5; ++t) {
@@ -278,7 +304,6 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
   cp_async_wait<kGroups - 1>();  // group 0: rows 0 .. 4
 #pragma unroll
   for (int rr = 0; rr < 4; ++rr) to_float2<S16>(stage[rr * 32 + lane], win[rr]);
-  uint8_t *d = j.dst + static_cast<int64_t>(y0) * j.dst_stride + 2 * e0;
 #pragma unroll 1
   for (int base = 0; base < rows; base += 5) {
     // Destination rows base .. base + 4 read source rows up to base + 8:
@@ -294,7 +319,9 @@ __device__ __forceinline__ void run_band16(const Sep16Job &j, uint4 *stage, int 
       if (base + S >= rows) return;  // past the band (the loop ends here)
       to_float2<S16>(stage[(base + S + 4) * 32 + lane], win[slot]);
       const uint4 out = filter_row<S16, S>(win, kx, ky);
-      if (outputs) {
+      if (SIMPLE) {
+        if (outputs) *reinterpret_cast<uint4 *>(d) = out;
+      } else if (outputs) {
         if (full_store) {
           *reinterpret_cast<uint4 *>(d) = out;
         } else {
