@@ -134,6 +134,31 @@ def test_gaussian_four_channel_streaming(kcv, oracle, ctx, k, sigma):
                                      f"off={offset}); first {bad[:4].tolist()}")
 
 
+@pytest.mark.parametrize("k,sigma", [(3, 0.8), (5, 1.1), (7, 1.5)])
+def test_gaussian_four_channel_unaligned_rows(kcv, oracle, ctx, k, sigma):
+    """The four-channel streaming Gaussian on rows that are 4-byte but not
+    16-byte aligned (every pixel copied on its own): row strides of w * 4
+    bytes with w % 4 != 0, base offsets of 4, 8 and 12 bytes, destinations
+    4-byte aligned (word stores) and not (bytes), every border; a base 2
+    bytes off (not whole pixels) takes the tiled kernel."""
+    rng = np.random.default_rng(70 + k)
+    cases = [(1366, 77, 0, 0), (723, 41, 4, 0), (1001, 23, 8, 1), (33, 100, 12, 0), (k + 1, k + 2, 4, 3),
+             (3841, 19, 0, 2), (517, 9, 2, 0)]
+    for i, (w, h, offset, dpad) in enumerate(cases):
+        for border in BORDERS + [0]:
+            host = padded(rng, h, w * 4, np.uint8, 0)
+            bv = int(rng.integers(0, 256)) if border == 0 else None
+            got, pad_ok = run_gaussian(kcv, ctx, host, w, h, 4, k, sigma, border, bv=bv, offset=offset,
+                                       dst_pad=dpad)
+            err, want = oracle.gaussian_blur_u8(host, w, h, 4, k, sigma, border, ext=bv is not None,
+                                                border_value=bv or 0, nthreads=8)
+            assert err == oracle.OK and pad_ok
+            if not np.array_equal(got, want):
+                bad = np.argwhere(got != want)
+                raise AssertionError(f"{len(bad)} mismatches (w={w} h={h} k={k} b={border} off={offset}); "
+                                     f"first {bad[:4].tolist()}")
+
+
 @pytest.mark.parametrize("offset", [1, 3, 8])
 def test_gaussian_misaligned_and_padded(kcv, oracle, ctx, offset):
     rng = np.random.default_rng(offset)

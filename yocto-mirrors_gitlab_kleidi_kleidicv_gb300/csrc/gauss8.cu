@@ -18,14 +18,17 @@
 // 16-byte cp.async per lane and row into its own shared-memory slots), in
 // copy groups of K rows that are filtered as they land, then streams down
 // the band: the unpacked rows of the vertical window stay in registers in
-// statically indexed slots (the row loop is unrolled by K).  The source must
-// be 16-byte aligned (other calls take the generic kernel).  Lanes whose 4
-// pixels lie inside the row copy them as one 16-byte piece; lanes at the
-// row's ends (left of pixel 0, or reaching past the last pixel) copy each of
-// their pixels from its border-mapped column with a 4-byte cp.async (the
-// border value for CONSTANT), so every stored pixel reads real neighbours and
-// the row ends need no separate pass.  Warps whose every lane stores whole
-// 16-byte pieces run a loop without the byte-store path.
+// statically indexed slots (the row loop is unrolled by K).  The source rows
+// must be 4-byte aligned (whole pixels; other calls take the generic
+// kernel).  With 16-byte aligned rows, lanes whose 4 pixels lie inside the
+// row copy them as one 16-byte piece; lanes at the row's ends (left of pixel
+// 0, or reaching past the last pixel), and every lane of rows that are not
+// 16-byte aligned, copy each of their pixels from its border-mapped column
+// with a 4-byte cp.async (the border value for CONSTANT), so every stored
+// pixel reads real neighbours and the row ends need no separate pass.  Warps
+// whose every lane stores whole 16-byte pieces run a loop without the
+// per-pixel store path, which writes 4-byte words where the destination
+// allows and bytes otherwise.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -161,7 +164,8 @@ __device__ __forceinline__ void run_band8(const Gauss8Job &j, uint4 *stage, int 
   const long e0 = static_cast<long>(strip) * kStripPix + kPix * lane - kPix;  // first pixel of the lane
   // Pixels needed by stored outputs: [-R, w + R).
   const bool live = e0 + kPix > -R && e0 < static_cast<long>(j.w) + R;
-  const bool fast = e0 >= 0 && e0 + kPix <= j.w;
+  const bool rows16 = ((reinterpret_cast<uintptr_t>(j.src) | static_cast<uintptr_t>(j.src_stride)) & 15) == 0;
+  const bool fast = rows16 && e0 >= 0 && e0 + kPix <= j.w;
   // Border lanes: the source column of each pixel (-1: the border value).
   int col[kPix];
 #pragma unroll
@@ -257,14 +261,19 @@ __device__ __forceinline__ void band_loop8(const Gauss8Job &j, const uint4 *stag
           *reinterpret_cast<uint4 *>(d) = out;
         } else {
           const uint32_t o[4] = {out.x, out.y, out.z, out.w};
+          const bool words = ((reinterpret_cast<uintptr_t>(j.dst) | static_cast<uintptr_t>(j.dst_stride)) & 3) == 0;
 #pragma unroll
           for (int p = 0; p < kPix; ++p)
             if (e0 + p < j.w) {
-              uint8_t *b = d + 4 * p;  // any alignment: bytes
-              b[0] = static_cast<uint8_t>(o[p]);
-              b[1] = static_cast<uint8_t>(o[p] >> 8);
-              b[2] = static_cast<uint8_t>(o[p] >> 16);
-              b[3] = static_cast<uint8_t>(o[p] >> 24);
+              uint8_t *b = d + 4 * p;
+              if (words) {
+                *reinterpret_cast<uint32_t *>(b) = o[p];
+              } else {  // any alignment: bytes
+                b[0] = static_cast<uint8_t>(o[p]);
+                b[1] = static_cast<uint8_t>(o[p] >> 8);
+                b[2] = static_cast<uint8_t>(o[p] >> 16);
+                b[3] = static_cast<uint8_t>(o[p] >> 24);
+              }
             }
         }
       }
@@ -328,7 +337,8 @@ cudaError_t launch8(Gauss8Job &j, int sm_count, cudaStream_t stream) {
 
 bool gauss8_eligible(const FilterJob &f) {
   if (f.mode != MODE_SIGMA || f.channels != 4 || (f.ksize != 3 && f.ksize != 5 && f.ksize != 7)) return false;
-  if (((reinterpret_cast<uintptr_t>(f.src) | static_cast<uintptr_t>(f.src_stride)) & 15) != 0) return false;
+  // Whole pixels: 4-byte cp.async of every source pixel.
+  if (((reinterpret_cast<uintptr_t>(f.src) | static_cast<uintptr_t>(f.src_stride)) & 3) != 0) return false;
   // Item indices in 32 bits.
   return static_cast<long>(f.height) * (f.width / kStripPix + 1) < (1L << 30);
 }
