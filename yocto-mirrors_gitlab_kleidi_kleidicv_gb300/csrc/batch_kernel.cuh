@@ -51,7 +51,9 @@ __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
     }
     uint32_t gstage = 0;
     const TmaMaps maps{&j.tmap, &j.tmap_row, &j.tmap_wrap, &j.tmap_wrap_row};
-    run_tile<MODE, K, C, NARROW>(j, maps, bt.strip, bt.band, smem, gstage, err_flag, timed_out);
+    // Without the aligned-block stores: the batched kernels measured faster
+    // without that code, unaligned destinations included.
+    run_tile<MODE, K, C, NARROW, false>(j, maps, bt.strip, bt.band, smem, gstage, err_flag, timed_out);
   }
 }
 

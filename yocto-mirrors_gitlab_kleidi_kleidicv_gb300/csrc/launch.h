@@ -81,6 +81,11 @@ void pyr_entry(PyrEntry &e, const uint8_t *src, int64_t src_stride, uint8_t *dst
 // a CUDA failure).
 int pyramid_warps(int channels, int sm_count);
 
+// Copies `height` rows of `row_bytes` bytes (any source alignment) into
+// `dst`, whose base and stride are multiples of 16 (realign.cu).
+cudaError_t launch_realign(const uint8_t *src, int64_t src_stride, uint8_t *dst, int64_t dst_stride,
+                           long row_bytes, int height, int sm_count, cudaStream_t stream);
+
 // Generic per-element two-pass Gaussian (arbitrary sizes 11..255, and any
 // generated kernel whose weights do not sum to 256).  `scratch` holds the
 // u8 intermediate image: width*channels bytes per row, `scratch_stride`

@@ -118,6 +118,39 @@ __device__ __forceinline__ bool load_chunk_fast(const uint8_t *row, long xb, lon
   return true;
 }
 
+// Stores a lane's 16 result bytes `r` at `d`, which lies m = d % 16 bytes past
+// a 16-byte boundary, as the aligned block [d - m, d + 16 - m): its first m
+// bytes are the last m of the previous lane's result `pr`.  The first lane
+// of a run (its previous lane stores nothing) writes bytes [0, 16 - m) of
+// its own result instead, and the last lane (its next lane stores nothing)
+// also writes bytes [16 - m, 16), which no block covers.
+__device__ __forceinline__ void store_shifted(uint8_t *d, const uint4 &pr, const uint4 &r, bool first, bool last) {
+  const int m = static_cast<int>(reinterpret_cast<uintptr_t>(d) & 15);
+  if (m == 0) {
+    *reinterpret_cast<uint4 *>(d) = r;
+    return;
+  }
+  if (!first) {
+    // Bytes [16 - m, 32 - m) of pr : r.
+    const uint32_t c[8] = {pr.x, pr.y, pr.z, pr.w, r.x, r.y, r.z, r.w};
+    const int s = 16 - m, q = s >> 2, s8 = (s & 3) * 8;
+    uint32_t o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t lo = q == 0 ? c[k] : q == 1 ? c[k + 1] : q == 2 ? c[k + 2] : c[k + 3];
+      const uint32_t hi = q == 0 ? c[k + 1] : q == 1 ? c[k + 2] : q == 2 ? c[k + 3] : c[k + 4];
+      o[k] = __funnelshift_r(lo, hi, s8);
+    }
+    *reinterpret_cast<uint4 *>(d - m) = make_uint4(o[0], o[1], o[2], o[3]);
+  }
+  if (first || last) {
+    const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (i < 16 - m ? first : last) d[i] = static_cast<uint8_t>(w[i >> 2] >> (8 * (i & 3)));
+  }
+}
+
 // Where the bytes of the tile rows live in shared memory.  The ring holds
 // ring_rows = stages * stage_rows rows; stage s of a tile occupies ring rows
 // [slot * stage_rows, slot * stage_rows + stage_rows) with slot = (g + s) mod
@@ -724,8 +757,10 @@ struct TmaMaps {
 // ---------------------------------------------------------------------------
 // One tile: strip `strip` x band `band` of job `j`.  `gstage` counts ring
 // stages used by this CTA so far (mbarrier phases continue across tiles).
-// stage_rows and stages are powers of two.
-template <int MODE, int K, int C, bool NARROW>
+// stage_rows and stages are powers of two.  SHIFT_STORES compiles the
+// aligned-block stores for destination rows that are not 16-byte aligned
+// (store_shifted); without it such rows are written byte by byte.
+template <int MODE, int K, int C, bool NARROW, bool SHIFT_STORES>
 __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps, int strip,
                                          int band, uint8_t *smem, uint32_t &gstage,
                                          int *err_flag, bool &timed_out) {
@@ -890,6 +925,16 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // This lane writes a whole 16-byte chunk with one vector store.
   const bool stores = emits && active && xb < wcb;
   const bool full_store = stores && dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
+  // Destination rows that are not 16-byte aligned: a lane whose chunk lies
+  // inside the row writes the aligned 16-byte block that ends inside its
+  // chunk, assembled from its own result and the previous lane's; the first
+  // and last such lanes of the warp also write the bytes of their chunk that
+  // no block covers (the modes with 16 destination bytes per chunk).
+  const bool shift_store = SHIFT_STORES && !ModeTraits<MODE>::SOBEL && MODE != MODE_BLURDOWN && stores &&
+                           !dst_rows_aligned && xb >= 0 && xb + kChunk <= wcb;
+  const unsigned shift_mask = SHIFT_STORES ? __ballot_sync(0xffffffffu, shift_store) : 0u;
+  const bool shift_first = shift_store && !((shift_mask >> (lane - 1)) & 1u);
+  const bool shift_last = shift_store && !((shift_mask >> (lane + 1)) & 1u);
   const uint32_t bv_elem = ES == 1 ? (static_cast<uint32_t>(j.border_value) & 0xFFu)
                                    : (static_cast<uint32_t>(j.border_value) & 0xFFFFu);
   const uint32_t bv_word = ES == 1 ? bv_elem * 0x01010101u : bv_elem * 0x00010001u;
@@ -1041,7 +1086,7 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
   // Lanes outside the interior compute a duplicate of their nearest interior
   // neighbour's horizontal pass (never stored), so that no branch is needed.
   const int hlane = min(max(lane, HC), 31 - HC);
-  const bool partial_store = stores && !full_store;
+  const bool partial_store = stores && !full_store && !shift_store;
   constexpr int NIN = block_in_rows(MODE, K);
 
   // ---- output rows in blocks of M.  Before a block, the stages holding only
@@ -1143,6 +1188,12 @@ __device__ __forceinline__ void run_tile(const FilterJob &j, const TmaMaps &maps
         uint8_t *drow = dblock + Mi * dst_stride;
         const bool row_ok = Mi < mcount;
         if (full_store && row_ok) *reinterpret_cast<uint4 *>(drow) = r;
+        if (SHIFT_STORES && shift_mask != 0u) {
+          // The previous lane's result ends where this lane's chunk begins.
+          const uint4 pr = make_uint4(__shfl_up_sync(0xffffffffu, r.x, 1), __shfl_up_sync(0xffffffffu, r.y, 1),
+                                      __shfl_up_sync(0xffffffffu, r.z, 1), __shfl_up_sync(0xffffffffu, r.w, 1));
+          if (shift_store && row_ok) store_shifted(drow, pr, r, shift_first, shift_last);
+        }
         if (partial_store && row_ok) {
           const uint32_t w4[4] = {r.x, r.y, r.z, r.w};
           for (int k = 0; k < kChunk && xb + k < wcb; ++k)
@@ -1196,7 +1247,7 @@ __global__ void __launch_bounds__(128, (K >= 15 ? 2 : 4))
   // above overlapped its tail).
   grid_dependency_wait();
   for (int t = blockIdx.x; t < tiles; t += gridDim.x)
-    run_tile<MODE, K, C, NARROW>(job, maps, t % job.strips, t / job.strips, smem, gstage,
+    run_tile<MODE, K, C, NARROW, true>(job, maps, t % job.strips, t / job.strips, smem, gstage,
                                  err_flag, timed_out);
 }
 
