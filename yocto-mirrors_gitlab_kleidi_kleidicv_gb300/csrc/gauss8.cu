@@ -19,8 +19,8 @@
 // copy groups of K rows that are filtered as they land, then streams down
 // the band: the unpacked rows of the vertical window stay in registers in
 // statically indexed slots (the row loop is unrolled by K).  The source rows
-// must be 4-byte aligned (whole pixels; other calls take the generic
-// kernel).  With 16-byte aligned rows, lanes whose 4 pixels lie inside the
+// must be 4-byte aligned (whole pixels; other calls take the tiled kernel of
+// sepfused.cuh).  With 16-byte aligned rows, lanes whose 4 pixels lie inside the
 // row copy them as one 16-byte piece; lanes at the row's ends (left of pixel
 // 0, or reaching past the last pixel), and every lane of rows that are not
 // 16-byte aligned, copy each of their pixels from its border-mapped column

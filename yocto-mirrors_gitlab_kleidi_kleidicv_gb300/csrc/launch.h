@@ -57,14 +57,15 @@ cudaError_t launch_fused_batch(const FilterJob &rep, const BatchLaunch &b, int *
 int fused_batch_blocks_per_sm(const FilterJob &rep, const BatchLaunch &b);
 
 // separable_filter_2d u16 / s16 with 5x5 kernels on one channel
-// (csrc/sep16.cu).  sep16_eligible: the job is of that kind, its addresses
-// allow 16-bit accesses, and (s16) the taps keep every sum exact in fp32.
+// (csrc/sep16.cu).  sep16_eligible: the job is of that kind, its source rows
+// are 16-byte aligned, its destination allows 16-bit stores, and (s16) the
+// taps keep every sum exact in fp32.
 bool sep16_eligible(const FilterJob &job);
 cudaError_t launch_sep16(const FilterJob &job, int sm_count, cudaStream_t stream);
 
 // gaussian_blur_u8 on four channels with generated 3x3 / 5x5 / 7x7 kernels
 // summing to 256 (csrc/gauss8.cu).  gauss8_eligible: the job is of that kind
-// and its source rows allow 16-byte copies.
+// and its source rows are 4-byte aligned (whole pixels).
 bool gauss8_eligible(const FilterJob &job);
 cudaError_t launch_gauss8(const FilterJob &job, int sm_count, cudaStream_t stream);
 

@@ -36,8 +36,9 @@
 // the band: the converted rows of the vertical window (five rows x 8 floats)
 // rotate through statically indexed register slots (the row loop is unrolled
 // by five), and each destination row costs one shared-memory load per lane.
-// The source must be 16-byte aligned (the host sends other calls to the
-// generic kernel).  This pass reads only the lanes whose 8 elements lie
+// The source rows must be 16-byte aligned (the host copies larger unaligned
+// sources into a 16-byte-row image first, and sends smaller ones to the
+// tiled kernel of sepfused.cuh).  This pass reads only the lanes whose 8 elements lie
 // inside the row, [0, wf) with wf = 8 * floor(w / 8), and stores only the
 // outputs whose five columns lie inside that span, x in [2, wf - 2).  The
 // other columns (x < 2 and x >= wf - 2) are edge elements, spread evenly over
