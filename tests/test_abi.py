@@ -231,3 +231,57 @@ def test_rows_beyond_32_bit_device_indexing_are_refused(lib, kcv):
     assert lib.kleidicv_gpu_sobel_3x3_horizontal_s16_u8(FAKE, big, FAKE, 2 * big, big // 2 + 8, 8, 1,
                                                         None) == kcv.RANGE
     assert lib.kleidicv_gpu_median_blur_u8(FAKE, big, FAKE + 16, big, big, 8, 1, 3, 3, 1, None) == kcv.RANGE
+
+
+def test_sme_twins_validate_like_their_base_entries(lib, kcv, no_gpu):
+    """The `_sme` twins (kleidicv.h:2010, 2054, 2097, 2109, 2165, 2220) return
+    exactly what their base entries return for calls that fail validation
+    (null pointers, unsupported sizes, borders and channel counts, sizes out
+    of range); validation runs before any device work."""
+    if not no_gpu:
+        pytest.skip("runs where no GPU can pick the calls up (the GPU twin tests cover the rest)")
+    t8 = (ctypes.c_uint8 * 5)(1, 2, 3, 2, 1)
+    t16 = (ctypes.c_uint16 * 5)(1, 2, 3, 2, 1)
+    big = 1 << 30
+    cases = {
+        "kleidicv_gpu_gaussian_blur_u8": [
+            (None, 64, FAKE, 64, 64, 8, 1, 5, 5, 0.0, 0.0, 2, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 1, 4, 4, 0.0, 0.0, 2, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 1, 5, 5, 0.0, 0.0, 0, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 5, 5, 5, 0.0, 0.0, 2, None),
+            (FAKE, big, FAKE, big, big, big, 1, 5, 5, 0.0, 0.0, 2, None),
+        ],
+        "kleidicv_gpu_separable_filter_2d_u8": [
+            (None, 64, FAKE, 64, 64, 8, 1, t8, 5, t8, 5, 2, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 1, t8, 3, t8, 3, 2, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 1, None, 5, t8, 5, 2, None),
+            (FAKE, 64, FAKE, 64, 64, 8, 1, t8, 5, t8, 5, 0, None),
+        ],
+        "kleidicv_gpu_separable_filter_2d_u16": [
+            (None, 128, FAKE, 128, 64, 8, 1, t16, 5, t16, 5, 2, None),
+            (FAKE, 128, FAKE, 128, 64, 8, 1, t16, 5, None, 5, 2, None),
+            (FAKE, 128, FAKE, 128, 64, 8, 5, t16, 5, t16, 5, 2, None),
+        ],
+        "kleidicv_gpu_blur_and_downsample_u8": [
+            (FAKE, 64, 64, 8, None, 32, 1, 2, None),
+            (FAKE, 64, 64, 8, FAKE, 32, 5, 2, None),
+            (FAKE, 64, 64, 8, FAKE, 32, 1, 0, None),
+        ],
+        "kleidicv_gpu_sobel_3x3_horizontal_s16_u8": [
+            (None, 64, FAKE, 128, 64, 8, 1, None),
+            (FAKE, 64, FAKE, 128, 64, 8, 5, None),
+        ],
+        "kleidicv_gpu_sobel_3x3_vertical_s16_u8": [
+            (FAKE, 64, None, 128, 64, 8, 1, None),
+            (FAKE, 64, FAKE, 128, 64, 8, 5, None),
+        ],
+    }
+    n = 0
+    for name, calls in cases.items():
+        base, twin = getattr(lib, name), getattr(lib, name + "_sme")
+        for args in calls:
+            want = base(*args)
+            assert want not in (kcv.OK, kcv.ERROR_NO_DEVICE), (name, args, want)
+            assert twin(*args) == want, (name, args)
+            n += 1
+    assert n == 19
