@@ -9,9 +9,11 @@
 // uploads the job table and the work-lists in one device allocation.  A
 // launch resets the work counters and starts one persistent kernel per group
 // on forked streams, so the groups run concurrently; blur-and-downsample
-// requests go to the pyramid kernel (one launch per channel count over an
-// entry table), and arbitrary-size Gaussians (two-pass kernel with a scratch
-// image) and copies run on a branch of their own.  With use_graph the whole
+// requests go to the pyramid kernel and four-channel generated 3x3 / 5x5 /
+// 7x7 Gaussians to the streaming kernel of gauss8.cu (one launch per channel
+// count or kernel size, over an entry table), and arbitrary-size Gaussians
+// (two-pass kernel with a scratch image) and copies run on a branch of their
+// own.  With use_graph the whole
 // launch is captured once into a CUDA graph and replayed.
 #include <string.h>
 
@@ -100,6 +102,9 @@ struct kleidicv_gpu_batch_plan {
   // while planning, then one single-phase pyramid launch over a device table.
   std::vector<kcv::PyrEntry> pyr[4];
   kcv::PyrEntry *d_pyr[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Four-channel generated Gaussians by kernel size (index (K - 3) / 2).
+  std::vector<kcv::Gauss8Job> g8[3];
+  kcv::Gauss8Job *d_g8[3] = {nullptr, nullptr, nullptr};
   uint8_t *dmem = nullptr;
   size_t dmem_bytes = 0;
   FilterJob *d_jobs = nullptr;
@@ -152,6 +157,13 @@ kleidicv_error_t enqueue(kleidicv_gpu_batch_plan *p, cudaStream_t s) {
     used[b] = true;
     e = launch_pyramid(L, ctx->sm_count, nb ? p->branches[b] : s);
   }
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    if (p->g8[k].empty()) continue;
+    const size_t b = nb ? lane++ % nb : 0;
+    used[b] = true;
+    e = launch_gauss8_batch(3 + 2 * k, p->d_g8[k], static_cast<int>(p->g8[k].size()), p->g8[k].back().item_end,
+                            ctx->sm_count, nb ? p->branches[b] : s);
+  }
   cudaStream_t tail = nb ? p->branches[nb - 1] : s;
   for (size_t i = 0; i < p->generic.size() && e == cudaSuccess; ++i) {
     e = launch_generic_gaussian(p->generic[i], p->dmem + p->generic_off[i], p->generic_stride[i], tail);
@@ -188,6 +200,7 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
   p->ctx = ctx;
 
   std::map<std::tuple<int, int, int, int>, size_t> group_of;
+  long g8_items_bound[3] = {0, 0, 0};
   size_t generic_bytes = 0;
   for (size_t i = 0; i < count; ++i) {
     Prepared pr;
@@ -210,6 +223,19 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
         break;
       }
       case Prepared::FUSED: {
+        if (gauss8_eligible(pr.fused)) {
+          // Item counts of a table stay in 32 bits: at most rows x strips items
+          // per request (bands <= rows), a group takes requests up to 2^30.
+          const int k = (pr.fused.ksize - 3) / 2;
+          const long most = static_cast<long>(pr.fused.height) * (pr.fused.width / kGauss8Lanes / 4 + 1);
+          if (g8_items_bound[k] + most < (1L << 30)) {
+            g8_items_bound[k] += most;
+            Gauss8Job g;
+            gauss8_job(pr.fused, g);  // bands sized once the request count is known
+            p->g8[k].push_back(g);
+            break;
+          }
+        }
         if (pr.fused.mode == MODE_BLURDOWN) {
           const FilterJob &f = pr.fused;
           PyrEntry en;
@@ -289,11 +315,28 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
     }
     pyr_bytes[c] = align_up(v.size() * sizeof(PyrEntry), 256);
   }
+  // Four-channel Gaussians: bands sized for each request's share of the
+  // streaming kernel's resident warps, items counted through the table.
+  size_t ng8_groups = 0, g8_bytes[3] = {0, 0, 0};
+  for (int k = 0; k < 3; ++k) {
+    std::vector<Gauss8Job> &v = p->g8[k];
+    if (v.empty()) continue;
+    ++ng8_groups;
+    const int share = std::max(1, gauss8_batch_warps(3 + 2 * k, ctx->sm_count) / static_cast<int>(v.size()));
+    int32_t items = 0;
+    for (Gauss8Job &g : v) {
+      gauss8_size_for_share(g, share);
+      items += g.strips * g.bands;
+      g.item_end = items;
+    }
+    g8_bytes[k] = align_up(v.size() * sizeof(Gauss8Job), 256);
+  }
   const size_t jobs_bytes = align_up(p->jobs.size() * sizeof(FilterJob), 256);
   const size_t tiles_bytes = align_up(all_tiles.size() * sizeof(BatchTile), 256);
   const size_t next_bytes = align_up(p->groups.size() * sizeof(int), 256);
   const size_t pyr_total = pyr_bytes[0] + pyr_bytes[1] + pyr_bytes[2] + pyr_bytes[3];
-  p->dmem_bytes = jobs_bytes + tiles_bytes + next_bytes + generic_bytes + pyr_total;
+  const size_t g8_total = g8_bytes[0] + g8_bytes[1] + g8_bytes[2];
+  p->dmem_bytes = jobs_bytes + tiles_bytes + next_bytes + generic_bytes + pyr_total + g8_total;
   if (p->dmem_bytes) {
     p->dmem = static_cast<uint8_t *>(ctx_alloc(ctx, p->dmem_bytes));
     if (!p->dmem) {
@@ -312,6 +355,11 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
       p->d_pyr[c] = reinterpret_cast<PyrEntry *>(p->dmem + off);
       off += pyr_bytes[c];
     }
+    for (int k = 0; k < 3; ++k) {
+      if (!g8_bytes[k]) continue;
+      p->d_g8[k] = reinterpret_cast<Gauss8Job *>(p->dmem + off);
+      off += g8_bytes[k];
+    }
   }
   // Through the pinned upload ring: no wait for the stream's earlier work.
   cudaError_t ce = upload_async(ctx, p->d_jobs, p->jobs.data(), p->jobs.size() * sizeof(FilterJob));
@@ -319,7 +367,9 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
     ce = upload_async(ctx, p->d_tiles, all_tiles.data(), all_tiles.size() * sizeof(BatchTile));
   for (int c = 0; c < 4 && ce == cudaSuccess; ++c)
     if (p->d_pyr[c]) ce = upload_async(ctx, p->d_pyr[c], p->pyr[c].data(), p->pyr[c].size() * sizeof(PyrEntry));
-  const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() + npyr_groups +
+  for (int k = 0; k < 3 && ce == cudaSuccess; ++k)
+    if (p->d_g8[k]) ce = upload_async(ctx, p->d_g8[k], p->g8[k].data(), p->g8[k].size() * sizeof(Gauss8Job));
+  const size_t nbranch = std::min<size_t>(kMaxBranches, p->groups.size() + npyr_groups + ng8_groups +
                                           ((p->generic.empty() && p->copies.empty()) ? 0 : 1));
   if (ce == cudaSuccess) {
     // The context's branch streams and events, created once and shared.
@@ -344,7 +394,7 @@ kleidicv_error_t kleidicv_gpu_batch_plan_create(const kleidicv_gpu_request_t *re
       p->joins.assign(ctx->branch_events.begin(), ctx->branch_events.begin() + nbranch);
     }
   }
-  p->kernels_per_launch = p->groups.size() + npyr_groups + 2 * p->generic.size();
+  p->kernels_per_launch = p->groups.size() + npyr_groups + ng8_groups + 2 * p->generic.size();
   if (ce != cudaSuccess) {
     kleidicv_gpu_batch_plan_destroy(p);
     return cuda_status(ctx, ce);

@@ -302,6 +302,52 @@ __global__ void __launch_bounds__(kThreadsG, K == 7 ? 4 : 5) gauss8_kernel(const
   }
 }
 
+// Batch plans: one launch over a table of jobs of the same K.  Warp item t
+// belongs to the first entry whose item_end exceeds t; the item boundaries
+// are cached in shared memory for that search (a table in global memory
+// would make every search a chain of dependent loads).
+constexpr int kG8SearchEntries = 512;
+
+template <int K>
+__global__ void __launch_bounds__(kThreadsG, K == 7 ? 4 : 5)
+    gauss8_batch_kernel(const Gauss8Job *__restrict__ E, int n) {
+  extern __shared__ __align__(16) uint4 stage8b[];
+  __shared__ int ends[kG8SearchEntries];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint4 *stage = stage8b + warp * (kWarpStage / 16);
+  const bool cached = n <= kG8SearchEntries;
+  if (cached)
+    for (int k = threadIdx.x; k < n; k += blockDim.x) ends[k] = E[k].item_end;
+  __syncthreads();
+  const int total = E[n - 1].item_end;
+  const int gw = warp * gridDim.x + blockIdx.x;
+  const int nw = gridDim.x * kWarpsG;
+  for (int t = gw; t < total; t += nw) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) / 2;
+      if ((cached ? ends[mid] : E[mid].item_end) > t) hi = mid;
+      else lo = mid + 1;
+    }
+    const Gauss8Job &j = E[lo];
+    const int local = t - (lo > 0 ? (cached ? ends[lo - 1] : E[lo - 1].item_end) : 0);
+    const int band = local / j.strips, q = local - band * j.strips;
+    const int strip = static_cast<int>((q + 7L * band) % j.strips);
+    run_band8<K>(j, stage, strip, band, lane);
+  }
+}
+
+// Bands of at most kGauss8MaxBand rows, as many as give `slots` warps the
+// same number of items (one wave of n items per warp).
+void size_bands8(Gauss8Job &j, long slots) {
+  j.strips = (j.w + kStripPix - 1) / kStripPix;
+  const long min_bands = (j.h + kGauss8MaxBand - 1) / kGauss8MaxBand;
+  const long per_warp = std::max(1L, (min_bands * j.strips + slots - 1) / slots);
+  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, per_warp * slots / j.strips)));
+  j.band_q = j.h / j.bands;
+  j.band_r = j.h % j.bands;
+}
+
 template <int K>
 cudaError_t launch8(Gauss8Job &j, int sm_count, cudaStream_t stream) {
   auto kern = gauss8_kernel<K>;
@@ -310,14 +356,8 @@ cudaError_t launch8(Gauss8Job &j, int sm_count, cudaStream_t stream) {
   if (err != cudaSuccess) return err;
   const long resident = static_cast<long>(occ) * std::max(sm_count, 1);
   const long slots = resident * kWarpsG;
-  j.strips = (j.w + kStripPix - 1) / kStripPix;
-  // Bands of at most kGauss8MaxBand rows, as many as give every resident warp
-  // the same number of items (one wave of n items per warp).
-  const long min_bands = (j.h + kGauss8MaxBand - 1) / kGauss8MaxBand;
-  const long per_warp = std::max(1L, (min_bands * j.strips + slots - 1) / slots);
-  j.bands = static_cast<int32_t>(std::min<long>(j.h, std::max(min_bands, per_warp * slots / j.strips)));
-  j.band_q = j.h / j.bands;
-  j.band_r = j.h % j.bands;
+  // Every resident warp gets the same number of items.
+  size_bands8(j, slots);
   const long items = static_cast<long>(j.strips) * j.bands;
   const long grid = std::max(1L, std::min(resident, (items + kWarpsG - 1) / kWarpsG));
   cudaLaunchConfig_t cfg = {};
@@ -341,6 +381,57 @@ bool gauss8_eligible(const FilterJob &f) {
   if (((reinterpret_cast<uintptr_t>(f.src) | static_cast<uintptr_t>(f.src_stride)) & 3) != 0) return false;
   // Item indices in 32 bits.
   return static_cast<long>(f.height) * (f.width / kStripPix + 1) < (1L << 30);
+}
+
+template <int K>
+int batch_warps8(int sm_count) {
+  int occ = 0;
+  if (resident_ctas_per_sm<gauss8_batch_kernel<K>>(kThreadsG, kSmemG, &occ) != cudaSuccess) return 0;
+  return occ * std::max(sm_count, 1) * kWarpsG;
+}
+
+template <int K>
+cudaError_t launch_batch8(const Gauss8Job *table, int n, long items, int sm_count, cudaStream_t stream) {
+  const int warps = batch_warps8<K>(sm_count);
+  if (warps == 0) return cudaErrorInvalidValue;
+  const long grid = std::max(1L, std::min<long>(warps / kWarpsG, (items + kWarpsG - 1) / kWarpsG));
+  gauss8_batch_kernel<K><<<static_cast<unsigned>(grid), kThreadsG, kSmemG, stream>>>(table, n);
+  return cudaGetLastError();
+}
+
+void gauss8_job(const FilterJob &f, Gauss8Job &j) {
+  j = Gauss8Job{};
+  j.src = f.src;
+  j.dst = f.dst;
+  j.src_stride = f.src_stride;
+  j.dst_stride = f.dst_stride;
+  j.w = f.width;
+  j.h = f.height;
+  j.border = f.border;
+  j.border_value = f.border_value;
+  for (int t = 0; t < f.ksize; ++t) j.w8[t] = static_cast<uint32_t>(f.wy[t]);
+}
+
+int gauss8_batch_warps(int ksize, int sm_count) {
+  switch (ksize) {
+    case 3: return batch_warps8<3>(sm_count);
+    case 5: return batch_warps8<5>(sm_count);
+    case 7: return batch_warps8<7>(sm_count);
+  }
+  return 0;
+}
+
+void gauss8_size_for_share(Gauss8Job &j, int warps) { size_bands8(j, std::max(warps, 1)); }
+
+cudaError_t launch_gauss8_batch(int ksize, const Gauss8Job *table, int n, long items, int sm_count,
+                                cudaStream_t stream) {
+  if (n <= 0 || items <= 0) return cudaSuccess;
+  switch (ksize) {
+    case 3: return launch_batch8<3>(table, n, items, sm_count, stream);
+    case 5: return launch_batch8<5>(table, n, items, sm_count, stream);
+    case 7: return launch_batch8<7>(table, n, items, sm_count, stream);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_gauss8(const FilterJob &f, int sm_count, cudaStream_t stream) {

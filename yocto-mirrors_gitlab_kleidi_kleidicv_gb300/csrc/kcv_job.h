@@ -127,6 +127,7 @@ struct Gauss8Job {
   uint32_t w8[7];          // the full kernel (symmetric), K entries
   int32_t strips, bands;   // warp items: strips x bands, band-major
   int32_t band_q, band_r;  // band b has band_q + (b < band_r) rows
+  int32_t item_end;        // batch tables: items of this and the earlier entries
 };
 
 // Blur-and-downsample levels (csrc/pyramid.cu).  One entry is one level of

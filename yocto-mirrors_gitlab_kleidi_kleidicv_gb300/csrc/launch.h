@@ -67,6 +67,14 @@ cudaError_t launch_sep16(const FilterJob &job, int sm_count, cudaStream_t stream
 // summing to 256 (csrc/gauss8.cu).  gauss8_eligible: the job is of that kind
 // and its source rows are 4-byte aligned (whole pixels).
 bool gauss8_eligible(const FilterJob &job);
+// Batch plans (gauss8.cu): the job's Gauss8Job; the resident warps of the
+// batched kernel for `ksize`; bands sized for `warps` warps; one launch over
+// a device table of n jobs of the same ksize holding `items` warp items.
+void gauss8_job(const FilterJob &f, Gauss8Job &j);
+int gauss8_batch_warps(int ksize, int sm_count);
+void gauss8_size_for_share(Gauss8Job &j, int warps);
+cudaError_t launch_gauss8_batch(int ksize, const Gauss8Job *table, int n, long items, int sm_count,
+                                cudaStream_t stream);
 cudaError_t launch_gauss8(const FilterJob &job, int sm_count, cudaStream_t stream);
 
 // blur_and_downsample_u8 levels (csrc/pyramid.cu): L.phases phases of
