@@ -46,7 +46,10 @@ def test_pool_cap_refuses_scratch_and_batch_memory():
     _, src, dst = _img(rng, w, h, c)
     ctx = kcv.Context(0, torch.cuda.current_stream().cuda_stream, pool_limit=1024)
     assert _arbitrary(ctx, src, dst, w, h, c) == kcv.ALLOCATION
-    req = kcv.make_request(kcv.OP_GAUSSIAN_BLUR_U8, src.data_ptr(), w * c, dst.data_ptr(), w * c, w, h, c, 7, 7,
+    # A three-channel request: its tiled-kernel job record (with tensor maps)
+    # and work-list exceed the 1 KiB cap (a four-channel 7x7 request would
+    # take a 256-byte entry of the streaming kernel's table).
+    req = kcv.make_request(kcv.OP_GAUSSIAN_BLUR_U8, src.data_ptr(), w * c, dst.data_ptr(), w * c, w, h, 3, 7, 7,
                            1.5, 1.5, border_type=kcv.REFLECT)
     with pytest.raises(RuntimeError, match="ALLOCATION"):
         kcv.BatchPlan([req], ctx)
